@@ -1,0 +1,199 @@
+"""fv2d_gb300 -- GB300-native (sm_103a) explicit finite-volume hydro step of
+mdelorme/fv2d, behind the C-ABI declared in include/fv2d_gpu.h.
+
+This module is a thin ctypes binding of that ABI, shaped like the
+reference's per-step functor calls (UpdateFunctor::update,
+ComputeDtFunctor::computeDt, consToPrim/checkNegatives, InitFunctor::init).
+Every call goes through the compiled library fv2d_gb300/lib/libfv2d_gpu.so;
+there is no CPU fallback: if the library is missing, loading raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from ._abi import (  # noqa: F401  (re-exported enums)
+    Params, PROBLEMS, ERROR_NAMES, as_float32,
+    HLL, HLLC, FSLP, BC_ABSORBING, BC_REFLECTING, BC_PERIODIC, TS_EULER, TS_RK2,
+    PCM, PCM_WB, PLM, MUSCL_HANCOCK, GRAV_NONE, GRAV_CONSTANT, GRAV_ANALYTICAL,
+    BCTC_NONE, BCTC_FIXED_TEMPERATURE, BCTC_FIXED_GRADIENT, TCM_CONSTANT, TCM_B02,
+)
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libfv2d_gpu.so")
+
+RUN_STEPS, RUN_DONE, RUN_SAVE, RUN_NUMERIC = 0, 1, 2, 3
+
+_dp = C.POINTER(C.c_double)
+_lib = None
+
+
+class Fv2dError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fv2d error {ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib():
+    """The loaded C-ABI library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m fv2d_gb300.build` "
+                               "(no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.fv2d_params_default.argtypes = [C.POINTER(Params)]
+        L.fv2d_params_default.restype = None
+        L.fv2d_params_size.restype = C.c_size_t
+        L.fv2d_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
+        L.fv2d_destroy.argtypes = [vp]
+        L.fv2d_set_stream.argtypes = [vp, vp]
+        L.fv2d_init_problem.argtypes = [vp, C.c_int]
+        L.fv2d_set_prim.argtypes = [vp, _dp]
+        L.fv2d_get_prim.argtypes = [vp, _dp]
+        L.fv2d_get_cons.argtypes = [vp, _dp]
+        L.fv2d_set_prim_device.argtypes = [vp, vp]
+        L.fv2d_get_prim_device.argtypes = [vp, vp]
+        L.fv2d_compute_dt.argtypes = [vp, _dp, _dp, _dp, _dp]
+        L.fv2d_update.argtypes = [vp, C.c_double]
+        L.fv2d_get_counters.argtypes = [vp, C.POINTER(C.c_uint64)]
+        L.fv2d_advance.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_int, _dp,
+                                   C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.fv2d_get_time.argtypes = [vp, _dp, C.POINTER(C.c_int)]
+        L.fv2d_set_time.argtypes = [vp, C.c_double, C.c_int]
+        L.fv2d_get_step_log.argtypes = [vp, _dp, C.c_int, C.POINTER(C.c_int)]
+        L.fv2d_last_error.argtypes = [vp]
+        L.fv2d_last_error.restype = C.c_char_p
+        L.fv2d_build_info.argtypes = [C.c_char_p, C.c_int]
+        _lib = L
+    return _lib
+
+
+def default_params(**overrides):
+    """The reference's effective defaults (float-rounded like its .ini
+    reader), with overrides.  Real-valued overrides are taken as given; use
+    as_float32() to mimic values read from an .ini file."""
+    p = Params()
+    lib().fv2d_params_default(C.byref(p))
+    return p.update(**overrides)
+
+
+def build_info():
+    buf = C.create_string_buffer(256)
+    lib().fv2d_build_info(buf, 256)
+    return buf.value.decode()
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Simulation:
+    """One simulation on one GPU (an fv2d_ctx)."""
+
+    def __init__(self, params, device=0):
+        self._lib = lib()
+        self.params = params.copy()
+        self.h = C.c_void_p()
+        rc = self._lib.fv2d_create(C.byref(self.params), device, C.byref(self.h))
+        if rc != 0:
+            raise Fv2dError(rc, self._lib.fv2d_last_error(None).decode())
+        self.nx, self.ny = params.Nx, params.Ny
+
+    def _check(self, rc):
+        if rc != 0:
+            raise Fv2dError(rc, self._lib.fv2d_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.fv2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_ptr):
+        self._check(self._lib.fv2d_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def init_problem(self, name):
+        pb = PROBLEMS[name] if isinstance(name, str) else int(name)
+        self._check(self._lib.fv2d_init_problem(self.h, pb))
+
+    def set_prim(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if q.shape != (self.ny, self.nx, 4):
+            raise ValueError(f"expected shape {(self.ny, self.nx, 4)}, got {q.shape}")
+        self._check(self._lib.fv2d_set_prim(self.h, _ptr(q)))
+
+    def set_prim_ptr(self, host_ptr):
+        self._check(self._lib.fv2d_set_prim(self.h, C.cast(C.c_void_p(host_ptr), _dp)))
+
+    def get_prim_ptr(self, host_ptr):
+        self._check(self._lib.fv2d_get_prim(self.h, C.cast(C.c_void_p(host_ptr), _dp)))
+
+    def set_prim_device(self, dev_ptr):
+        self._check(self._lib.fv2d_set_prim_device(self.h, C.c_void_p(dev_ptr)))
+
+    def get_prim_device(self, dev_ptr):
+        self._check(self._lib.fv2d_get_prim_device(self.h, C.c_void_p(dev_ptr)))
+
+    def get_prim(self):
+        q = np.empty((self.ny, self.nx, 4))
+        self._check(self._lib.fv2d_get_prim(self.h, _ptr(q)))
+        return q
+
+    def get_cons(self):
+        u = np.empty((self.ny, self.nx, 4))
+        self._check(self._lib.fv2d_get_cons(self.h, _ptr(u)))
+        return u
+
+    def compute_dt(self):
+        """(dt, inv_dt_hyp, inv_dt_tc, inv_dt_visc) -- ComputeDtFunctor::computeDt."""
+        v = [C.c_double() for _ in range(4)]
+        self._check(self._lib.fv2d_compute_dt(self.h, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def update(self, dt):
+        """update(Q, U, dt) + consToPrim + checkNegatives (asynchronous)."""
+        self._check(self._lib.fv2d_update(self.h, float(dt)))
+
+    def counters(self):
+        c = (C.c_uint64 * 3)()
+        self._check(self._lib.fv2d_get_counters(self.h, c))
+        return list(c)
+
+    def advance(self, max_steps, tend, next_save=-1.0, skip_first_save_check=False):
+        """Device-driven main loop; returns (t, steps_done, status)."""
+        t = C.c_double()
+        n = C.c_int()
+        s = C.c_int()
+        rc = self._lib.fv2d_advance(self.h, int(max_steps), float(tend), float(next_save),
+                                    1 if skip_first_save_check else 0, C.byref(t), C.byref(n), C.byref(s))
+        if rc != 0 and s.value != RUN_NUMERIC:
+            self._check(rc)
+        return t.value, n.value, s.value
+
+    def time(self):
+        t = C.c_double()
+        it = C.c_int()
+        self._check(self._lib.fv2d_get_time(self.h, C.byref(t), C.byref(it)))
+        return t.value, it.value
+
+    def set_time(self, t, iteration):
+        self._check(self._lib.fv2d_set_time(self.h, float(t), int(iteration)))
+
+    def step_log(self, max_records=4096):
+        rec = np.empty((max_records, 3))
+        n = C.c_int()
+        self._check(self._lib.fv2d_get_step_log(self.h, _ptr(rec), max_records, C.byref(n)))
+        return rec[: n.value].copy()

@@ -1,0 +1,106 @@
+"""Builds the native parts of fv2d_gb300 in-tree for GB300 (sm_103a):
+
+  fv2d_gb300/lib/libfv2d_gpu.so   the C-ABI library (include/fv2d_gpu.h)
+
+Translation units are compiled in parallel with nvcc (one -gencode,
+arch=compute_103a,code=sm_103a); object files go to fv2d_gb300/_build/.
+Rebuilds only what changed (source or any header newer than the object).
+The FP64 step is compiled with -fmad=false so that no multiply-add is
+contracted: its results are then bit-identical to the reference's
+binary64 expressions.  Host C++ uses -ffp-contract=off for the same reason
+(GCC contracts by default on aarch64).
+"""
+import glob
+import os
+import platform
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIBDIR = os.path.join(PKG, "lib")
+LIB = os.path.join(LIBDIR, "libfv2d_gpu.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build fv2d_gb300")
+
+
+# (source, extra flags)
+UNITS = [
+    ("fv2d_api.cu", ["-fmad=false"]),
+    ("step_dispatch.cu", []),
+    ("step_hll.cu", ["-fmad=false"]),
+    ("step_hllc.cu", ["-fmad=false"]),
+    ("step_fslp.cu", ["-fmad=false"]),
+    ("problems.cpp", []),
+]
+
+
+def _headers():
+    return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
+        glob.glob(os.path.join(REPO, "include", "*.h"))
+
+
+def _stale(obj, src, hdr_mtime):
+    if not os.path.exists(obj):
+        return True
+    m = os.path.getmtime(obj)
+    return os.path.getmtime(src) > m or hdr_mtime > m
+
+
+def _compile(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def build(verbose=False, jobs=None):
+    """Compile every translation unit and link libfv2d_gpu.so.  Returns the
+    library path."""
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    nvcc = _nvcc()
+    hdr_mtime = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(__file__)])
+    # objects built on another host architecture are never reused
+    stamp = os.path.join(BUILD, "host-arch")
+    arch = platform.machine()
+    if not os.path.exists(stamp) or open(stamp).read().strip() != arch:
+        for f in glob.glob(os.path.join(BUILD, "*.o")) + [LIB]:
+            if os.path.exists(f):
+                os.unlink(f)
+        with open(stamp, "w") as f:
+            f.write(arch)
+    cmds, objs = [], []
+    for src, extra in UNITS:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+        objs.append(o)
+        if not _stale(o, s, hdr_mtime):
+            continue
+        if src.endswith(".cu"):
+            cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                   *extra, "-c", s, "-o", o]
+        else:
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", s, "-o", o]
+        cmds.append(cmd)
+    if cmds:
+        with ThreadPoolExecutor(max_workers=jobs or min(8, len(cmds))) as ex:
+            for out in ex.map(_compile, cmds):
+                if verbose and out.strip():
+                    print(out)
+    if cmds or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+        _compile([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fPIC"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -1,0 +1,270 @@
+// physics.cuh -- pointwise state math and Riemann solvers of the fv2d hydro
+// step, for device code (and host code where marked __host__).
+//
+// Every expression keeps the operand order of the reference so that, built
+// with -fmad=false, binary64 results are bit-identical to it:
+//   primToCons / consToPrim / speedOfSound   States.h:19-46
+//   hll                                      RiemannSolvers.h:7-51
+//   hllc                                     RiemannSolvers.h:53-128
+//   fslp                                     RiemannSolvers.h:130-171
+//   minmod                                   Update.h:77-85
+// Differences from the reference are in control flow only: the Riemann
+// solvers evaluate their candidate fluxes without data-dependent branches
+// and select at the end (same values, no warp divergence), and constants such
+// as 1/(gamma-1) are computed once by the caller with the same operation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fv2d {
+
+enum { IR = 0, IU = 1, IV = 2, IP = 3, IE = 3 };
+
+template <class R>
+struct S4 {
+  R r, u, v, p;  // (rho, u, v, p) or (rho, rho u, rho v, E)
+};
+
+// Per-simulation constants used by the pointwise functions.
+template <class R>
+struct Gas {
+  R gamma;   // gamma0
+  R gm1;     // gamma0 - 1.0
+  R entho;   // 1.0 / (gamma0 - 1.0)               (RiemannSolvers.h:76)
+  R fslp_K;  // FSLP K                              (SimInfo.h:399)
+};
+
+// States.h:19-30
+template <class R>
+__host__ __device__ __forceinline__ S4<R> prim_to_cons(const S4<R> &q, const Gas<R> &g) {
+  S4<R> s;
+  s.r = q.r;
+  s.u = q.r * q.u;
+  s.v = q.r * q.v;
+  R Ek = R(0.5) * (s.u * s.u + s.v * s.v) / q.r;
+  s.p = (Ek + q.p / g.gm1);
+  return s;
+}
+
+// States.h:32-43
+template <class R>
+__host__ __device__ __forceinline__ S4<R> cons_to_prim(const S4<R> &u, const Gas<R> &g) {
+  S4<R> q;
+  q.r = u.r;
+  q.u = u.u / u.r;
+  q.v = u.v / u.r;
+  R Ek = R(0.5) * q.r * (q.u * q.u + q.v * q.v);
+  q.p = (u.p - Ek) * g.gm1;
+  return q;
+}
+
+template <class R>
+__device__ __forceinline__ R dsqrt(R x) {
+  return sqrt(x);
+}
+
+// States.h:45-46
+template <class R>
+__device__ __forceinline__ R sound_speed(const S4<R> &q, const Gas<R> &g) {
+  return dsqrt(q.p * g.gamma / q.r);
+}
+
+// Update.h:77-85
+template <class R>
+__host__ __device__ __forceinline__ R minmod(R dL, R dR) {
+  R m = (fabs(dL) < fabs(dR)) ? dL : dR;
+  return (dL * dR < R(0)) ? R(0) : m;
+}
+
+template <class R>
+__device__ __forceinline__ R sel(bool c, R a, R b) {
+  return c ? a : b;
+}
+
+// RiemannSolvers.h:7-51.  All three candidates are evaluated, then selected
+// in the reference's branch order (SL >= 0, SR <= 0, else the HLL state).
+template <class R>
+__device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, const Gas<R> &g) {
+  const R aL = sound_speed(qL, g);
+  const R aR = sound_speed(qR, g);
+  const R sminL = qL.u - aL;
+  const R smaxL = qL.u + aL;
+  const R sminR = qR.u - aR;
+  const R smaxR = qR.u + aR;
+  const R SL = fmin(sminL, sminR);
+  const R SR = fmax(smaxL, smaxR);
+  // computeFlux (RiemannSolvers.h:133-141).  p/(gamma-1) is also the pressure
+  // term of primToCons below: the same division, evaluated once.
+  const R peL = qL.p / g.gm1;
+  const R peR = qR.p / g.gm1;
+  const R EkL = R(0.5) * qL.r * (qL.u * qL.u + qL.v * qL.v);
+  const R EkR = R(0.5) * qR.r * (qR.u * qR.u + qR.v * qR.v);
+  const R EL = (peL + EkL);
+  const R ER = (peR + EkR);
+  const R ruL = qL.r * qL.u, ruR = qR.r * qR.u;
+  S4<R> FL{ruL, ruL * qL.u + qL.p, ruL * qL.v, (qL.p + EL) * qL.u};
+  S4<R> FR{ruR, ruR * qR.u + qR.p, ruR * qR.v, (qR.p + ER) * qR.u};
+  // primToCons (States.h:19-30) of both states
+  const R mvL = qL.r * qL.v, mvR = qR.r * qR.v;
+  const R uEL = (R(0.5) * (ruL * ruL + mvL * mvL) / qL.r + peL);
+  const R uER = (R(0.5) * (ruR * ruR + mvR * mvR) / qR.r + peR);
+  const R SLSR = SL * SR;
+  const R den = SR - SL;
+  S4<R> FM;
+  FM.r = (SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r)) / den;
+  FM.u = (SR * FL.u - SL * FR.u + SLSR * (ruR - ruL)) / den;
+  FM.v = (SR * FL.v - SL * FR.v + SLSR * (mvR - mvL)) / den;
+  FM.p = (SR * FL.p - SL * FR.p + SLSR * (uER - uEL)) / den;
+  const R pM = R(0.5) * (qL.p + qR.p);
+  const bool left = (SL >= R(0));
+  const bool right = !left && (SR <= R(0));
+  f.r = left ? FL.r : (right ? FR.r : FM.r);
+  f.u = left ? FL.u : (right ? FR.u : FM.u);
+  f.v = left ? FL.v : (right ? FR.v : FM.v);
+  f.p = left ? FL.p : (right ? FR.p : FM.p);
+  pout = left ? qL.p : (right ? qR.p : pM);
+}
+
+// RiemannSolvers.h:53-128.  The star state is evaluated once, for the side
+// the reference would pick if it reaches the star branches (uS > 0 -> left,
+// otherwise right), then the final state is chosen in the reference's order.
+template <class R>
+__device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, const Gas<R> &g) {
+  const R rL = qL.r, uL = qL.u, vL = qL.v, pL = qL.p;
+  const R rR = qR.r, uR = qR.u, vR = qR.v, pR = qR.p;
+  const R ekL = R(0.5) * rL * (uL * uL + vL * vL);
+  const R EL = ekL + pL * g.entho;
+  const R ekR = R(0.5) * rR * (uR * uR + vR * vR);
+  const R ER = ekR + pR * g.entho;
+  const R cL = sound_speed(qL, g);
+  const R cR = sound_speed(qR, g);
+  const R cmax = fmax(cL, cR);
+  const R SL = fmin(uL, uR) - cmax;
+  const R SR = fmax(uL, uR) + cmax;
+  const R rcL = rL * (uL - SL);
+  const R rcR = rR * (SR - uR);
+  const R uS = (rcR * uR + rcL * uL + (pL - pR)) / (rcR + rcL);
+  const R pS = (rcR * pL + rcL * pR + rcL * rcR * (uL - uR)) / (rcR + rcL);
+  const bool sideL = (uS > R(0));
+  const R rK = sideL ? rL : rR;
+  const R uK = sideL ? uL : uR;
+  const R pK = sideL ? pL : pR;
+  const R EK = sideL ? EL : ER;
+  const R SK = sideL ? SL : SR;
+  const R rS = rK * (SK - uK) / (SK - uS);
+  const R ES = ((SK - uK) * EK - pK * uK + pS * uS) / (SK - uS);
+  // branch order of RiemannSolvers.h:89-112
+  const bool bL = (SL > R(0));
+  const bool bStar = !bL && (sideL || SR > R(0));
+  R sr, su, sv, sp, E;
+  if (bL) {
+    sr = rL; su = uL; sv = vL; sp = pL; E = EL;
+  } else if (bStar) {
+    sr = rS; su = uS; sv = sideL ? vL : vR; sp = pS; E = ES;
+  } else {
+    sr = rR; su = uR; sv = vR; sp = pR; E = ER;
+  }
+  pout = sp;
+  f.r = sr * su;
+  f.u = sr * su * su + sp;
+  f.v = f.r * sv;
+  f.p = (E + sp) * su;
+}
+
+// RiemannSolvers.h:130-171 (Kokkos::max / min as (a<b)?b:a and (b<a)?b:a).
+template <class R>
+__device__ __forceinline__ void riemann_fslp(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, R gdx,
+                                             const Gas<R> &g) {
+  const R rhoL = qL.r, uL = qL.u, pL = qL.p;
+  const R csL = dsqrt(g.gamma * pL / rhoL);
+  const R rhoR = qR.r, uR = qR.u, pR = qR.p;
+  const R csR = dsqrt(g.gamma * pR / rhoR);
+  const R zL = rhoL * csL, zR = rhoR * csR;
+  const R ai = g.fslp_K * ((zL < zR) ? zR : zL);
+  const R mL = fabs(uL) / csL, mR = fabs(uR) / csR;
+  const R mx = (mL < mR) ? mR : mL;
+  const R theta = (mx < R(1)) ? mx : R(1);
+  const R ustar = R(0.5) * (uR + uL) - R(0.5) / ai * (pR - pL - R(0.5) * (rhoL + rhoR) * gdx);
+  const R Pi = R(0.5) * (pR + pL) - theta * R(0.5) * ai * (uR - uL);
+  const bool up = ustar > R(0);
+  const R sr = up ? qL.r : qR.r;
+  const R su = up ? qL.u : qR.u;
+  const R sv = up ? qL.v : qR.v;
+  const R sp = up ? qL.p : qR.p;
+  const R Ekstar = R(0.5) * sr * (su * su + sv * sv);
+  const R Estar = Ekstar + sp / g.gm1;
+  f.r = ustar * sr;
+  f.u = ustar * sr * su + Pi;
+  f.v = ustar * sr * sv;
+  f.p = ustar * (Estar + Pi);
+  pout = Pi;
+}
+
+enum { RS_HLL = 0, RS_HLLC = 1, RS_FSLP = 2 };
+
+template <int RS, class R>
+__device__ __forceinline__ void riemann(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, R gdx, const Gas<R> &g) {
+  if constexpr (RS == RS_HLL)
+    riemann_hll(qL, qR, f, pout, g);
+  else if constexpr (RS == RS_FSLP)
+    riemann_fslp(qL, qR, f, pout, gdx, g);
+  else
+    riemann_hllc(qL, qR, f, pout, g);
+}
+
+// Extension (no reference counterpart): primitive-variable MUSCL-Hancock
+// half-step qh = q - (dt/2dx) A(q) sx - (dt/2dy) B(q) sy, with ax = 0.5 dt/dx,
+// ay = 0.5 dt/dy and sx, sy the full minmod slopes.
+template <class R>
+__host__ __device__ __forceinline__ S4<R> hancock(const S4<R> &q, const S4<R> &sx, const S4<R> &sy, R ax, R ay,
+                                                  R gamma) {
+  S4<R> h;
+  h.r = q.r - (ax * (q.u * sx.r + q.r * sx.u) + ay * (q.v * sy.r + q.r * sy.v));
+  h.u = q.u - (ax * (q.u * sx.u + sx.p / q.r) + ay * (q.v * sy.u));
+  h.v = q.v - (ax * (q.u * sx.v) + ay * (q.v * sy.v + sy.p / q.r));
+  h.p = q.p - (ax * (gamma * q.p * sx.u + q.u * sx.p) + ay * (gamma * q.p * sy.v + q.v * sy.p));
+  return h;
+}
+
+// ---------------------------------------------------------------- boundaries
+// Source (interior index, 0-based) of ghost `k` along one axis of length N,
+// for the boundary fills of BoundaryConditions.h:13-71.  Ghost indices are
+// interior-relative: -2, -1 on the low side, N, N+1 on the high side.
+// Returns the source index and sets *neg when the normal velocity flips
+// (reflecting walls).
+__host__ __device__ __forceinline__ int ghost_source(int k, int N, int bc, bool *neg) {
+  *neg = false;
+  if (k < 0) {
+    if (bc == 1) {  // reflecting: 2*ibeg - i - 1
+      *neg = true;
+      return -k - 1;
+    }
+    if (bc == 2) return k + N;  // periodic
+    return 0;                   // absorbing: copy ibeg
+  }
+  if (bc == 1) {
+    *neg = true;
+    return 2 * N - k - 1;
+  }
+  if (bc == 2) return k - N;
+  return N - 1;
+}
+
+// Ghost positions (interior-relative) whose source is interior index s;
+// returns their count (<= 4) in out[], with the matching negation flags.
+__host__ __device__ __forceinline__ int ghost_targets(int s, int N, int bc, int out[4], bool neg[4]) {
+  const int ks[4] = {-2, -1, N, N + 1};
+  int n = 0;
+  for (int t = 0; t < 4; ++t) {
+    bool ng;
+    if (ghost_source(ks[t], N, bc, &ng) == s) {
+      out[n] = ks[t];
+      neg[n] = ng;
+      ++n;
+    }
+  }
+  return n;
+}
+
+}  // namespace fv2d

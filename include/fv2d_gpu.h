@@ -1,0 +1,128 @@
+/*
+ * fv2d_gpu.h -- C-ABI of the GB300 (sm_103a) explicit hydro step,
+ * libfv2d_gpu.so.
+ *
+ * The reference has no FFI: its per-step boundary is the in-binary C++
+ * functor API called from main.cpp.  Each entry point below replaces one of
+ * those calls and keeps its argument meaning:
+ *
+ *   fv2d_create / fv2d_destroy      <- readInifile + View allocation
+ *                                      (SimInfo.h:529-568, main.cpp:33-34)
+ *                                      and the functor constructors
+ *                                      (Update.h:50-56, ComputeDt.h:15)
+ *   fv2d_init_problem               <- InitFunctor::init + primToCons
+ *                                      (Init.h:310-358, main.cpp:58)
+ *   fv2d_set_prim / fv2d_get_prim   <- loadSnapshot copy-in / saveSolution
+ *                                      copy-out (IOManager.h:358-379,
+ *                                      IOManager.h:244-262)
+ *   fv2d_compute_dt                 <- ComputeDtFunctor::computeDt
+ *                                      (ComputeDt.h:18-65)
+ *   fv2d_update                     <- UpdateFunctor::update + consToPrim +
+ *                                      checkNegatives (Update.h:193-222,
+ *                                      SimInfo.h:576-646, main.cpp:79-81)
+ *   fv2d_get_counters               <- the three counts printed by
+ *                                      checkNegatives (SimInfo.h:637-645)
+ *   fv2d_advance                    <- the whole main.cpp:62-84 loop body,
+ *                                      iterated on the device without host
+ *                                      round trips (stops at tend or at a
+ *                                      snapshot time)
+ *
+ * Conventions: every function returns an FV2D_* status (fv2d_types.h); no
+ * C++ exception crosses the ABI.  A context is not thread-safe; separate
+ * contexts are independent.  Host arrays use the interior row-major layout
+ * described in fv2d_types.h.  All work is queued on the context's stream;
+ * functions that return host values synchronise that stream.
+ */
+#ifndef FV2D_GPU_H
+#define FV2D_GPU_H
+
+#include "fv2d_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fv2d_ctx fv2d_ctx;
+
+/* Reference defaults (SimInfo.h:356-459, 529-552) exactly as the reference
+ * holds them after reading an .ini that leaves them unset: real-valued
+ * parameters pass through INIReader::GetFloat and are therefore
+ * float-rounded (gamma0 = (float)(5/3), CFL = 0.8f, ...). */
+void fv2d_params_default(fv2d_params *p);
+
+/* Validates p, selects device `device` (-1: current), allocates the state
+ * (two primitive buffers, the conservative buffer, RK2 stage buffer when
+ * time_stepping == RK2) and builds the TMA descriptors. */
+int fv2d_create(const fv2d_params *p, int device, fv2d_ctx **out);
+int fv2d_destroy(fv2d_ctx *ctx);
+
+/* Work is queued on this stream (a cudaStream_t; NULL = the context's own
+ * stream). */
+int fv2d_set_stream(fv2d_ctx *ctx, void *stream);
+
+/* Initial condition `problem` (FV2D_PB_*) computed on the host in binary64,
+ * uploaded, then boundary fill, primToCons and the dt reduction. */
+int fv2d_init_problem(fv2d_ctx *ctx, int problem);
+
+/* Interior primitive state (Ny x Nx x {rho,u,v,p}) from / to host memory.
+ * set_prim behaves like a restart: boundary fill, primToCons, dt reduction.
+ * Page-locked host memory gives full copy bandwidth. */
+int fv2d_set_prim(fv2d_ctx *ctx, const double *q_host);
+int fv2d_get_prim(fv2d_ctx *ctx, double *q_host);
+/* Interior conservative state (rho, rho u, rho v, E). */
+int fv2d_get_cons(fv2d_ctx *ctx, double *u_host);
+
+/* Same as set_prim / get_prim with device-resident interleaved arrays. */
+int fv2d_set_prim_device(fv2d_ctx *ctx, const double *q_dev);
+int fv2d_get_prim_device(fv2d_ctx *ctx, double *q_dev);
+
+/* ComputeDtFunctor::computeDt of the current primitive state:
+ * dt = CFL / max(inv_dt_hyp, inv_dt_tc, inv_dt_visc).  Any output pointer
+ * may be NULL.  The reductions are folded into the previous update (or the
+ * set_prim / init_problem pass), so this call only reads them back. */
+int fv2d_compute_dt(fv2d_ctx *ctx, double *dt, double *inv_dt_hyp, double *inv_dt_tc, double *inv_dt_visc);
+
+/* One reference iteration body with the caller's dt: update(Q, U, dt),
+ * consToPrim(U, Q), checkNegatives(Q).  Asynchronous. */
+int fv2d_update(fv2d_ctx *ctx, double dt);
+
+/* {negative density, negative pressure, NaN count} found by the
+ * checkNegatives of the last update.  Synchronises. */
+int fv2d_get_counters(fv2d_ctx *ctx, uint64_t out[3]);
+
+/* Device-driven main loop.  Runs at most max_steps iterations of
+ *   while (t + epsilon < tend) { [stop if t + epsilon > next_save];
+ *                                dt = computeDt; update; t += dt; }
+ * entirely on the GPU (CUDA-graph replays of the fused step), then
+ * synchronises.  next_save < 0 disables the snapshot stop.  When
+ * skip_first_save_check is non-zero the snapshot test is skipped for the first
+ * iteration (the caller just wrote that snapshot).  On return *t, *steps_done
+ * and *status (FV2D_RUN_*) describe where the loop stopped. */
+enum { FV2D_RUN_STEPS = 0, FV2D_RUN_DONE = 1, FV2D_RUN_SAVE = 2, FV2D_RUN_NUMERIC = 3 };
+int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, int skip_first_save_check,
+                 double *t, int *steps_done, int *status);
+
+/* Simulation clock kept on the device (t after the last committed update,
+ * iteration count).  set_time resets both (e.g. after a restart). */
+int fv2d_get_time(fv2d_ctx *ctx, double *t, int *iteration);
+int fv2d_set_time(fv2d_ctx *ctx, double t, int iteration);
+
+/* Per-iteration record of the last fv2d_advance call: for each iteration
+ * {t before the update, dt, inv_dt_hyp}; returns the number of records
+ * written (at most max_records). */
+int fv2d_get_step_log(fv2d_ctx *ctx, double *records, int max_records, int *count);
+
+/* Human-readable message of the last failure on this context (never NULL). */
+const char *fv2d_last_error(fv2d_ctx *ctx);
+
+/* Static description of the compiled kernels: writes a short text (tile
+ * shape, threads per block, architecture) into buf. */
+int fv2d_build_info(char *buf, int len);
+
+/* sizeof(fv2d_params) as compiled into the library. */
+size_t fv2d_params_size(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FV2D_GPU_H */

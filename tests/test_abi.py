@@ -1,0 +1,82 @@
+"""C-ABI checks that need no GPU: the library builds and loads, exports every
+entry point declared in include/*.h, and agrees with the Python mirror of the
+parameter block."""
+import ctypes as C
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+from fv2d_testlib import REPO, reference_params
+from fv2d_gb300 import _abi
+
+
+@pytest.fixture(scope="module")
+def libs():
+    from fv2d_gb300 import build as b
+    b.build()
+    import fv2d_gb300
+    return fv2d_gb300.lib()
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(fv2d_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_exports_every_declared_symbol(libs):
+    names = declared_functions()
+    assert "fv2d_create" in names and "fv2d_update" in names and "fv2d_compute_dt" in names
+    from fv2d_gb300 import LIB_PATH
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (fv2d_\w+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert hasattr(libs, n)
+
+
+def test_params_layout_matches_header(libs):
+    assert libs.fv2d_params_size() == C.sizeof(_abi.Params)
+    text = open(os.path.join(REPO, "include", "fv2d_types.h")).read()
+    body = text[text.index("typedef struct fv2d_params {"):text.index("} fv2d_params;")]
+    fields = []
+    for line in body.splitlines()[1:]:
+        line = re.sub(r"/\*.*?\*/", "", line).strip()
+        m = re.match(r"(uint32_t|int32_t|double)\s+(.*);", line)
+        if m:
+            fields += [(n.strip(), m.group(1)) for n in m.group(2).split(",")]
+    ctypes_of = {"uint32_t": C.c_uint32, "int32_t": C.c_int32, "double": C.c_double}
+    assert [(n, ctypes_of[t]) for n, t in fields] == list(_abi.Params._fields_)
+
+
+def test_defaults_are_the_references_effective_values(libs):
+    from fv2d_gb300 import default_params
+    p = default_params()
+    r = reference_params()
+    for name, _ in _abi.Params._fields_:
+        assert getattr(p, name) == getattr(r, name), name
+    assert p.gamma0 == float(C.c_float(5.0 / 3.0).value)
+    assert p.CFL == float(C.c_float(0.8).value)
+
+
+def test_build_info(libs):
+    from fv2d_gb300 import build_info
+    s = build_info()
+    assert "sm_103a" in s and "TMA" in s
+
+
+def test_create_rejects_bad_params_without_gpu(libs):
+    """Validation happens before any CUDA call."""
+    from fv2d_gb300 import Fv2dError, Simulation, default_params
+    for bad in (dict(Nx=1), dict(Nghosts=1), dict(riemann_solver=7), dict(boundary_x=5), dict(xmax=-1.0)):
+        with pytest.raises(Fv2dError) as e:
+            Simulation(default_params(**bad))
+        assert e.value.code == _abi.ERR_INVALID

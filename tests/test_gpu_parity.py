@@ -1,0 +1,217 @@
+"""GPU parity of the plain FP64 path, through the C-ABI.
+
+The bar is bit-identical binary64 results: every dt and every primitive
+value equal to the reference's (golden fixtures from the reference's own
+headers) and to the oracle (same seeded inputs), including odd grid sizes
+that cut tiles, every switch combination and the device-driven loop.  At the
+full benchmark size (2048^2) the GPU is compared bitwise with the OpenMP
+oracle for a few iterations, and checked for exact mass conservation
+properties and run-to-run determinism.
+"""
+import numpy as np
+import pytest
+
+import golden.make_golden as G
+from fv2d_testlib import Oracle, bits_equal, random_prim, reference_params
+from test_oracle import negative_case
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_sim(p):
+    from fv2d_gb300 import Simulation
+    return Simulation(p)
+
+
+def test_combos_match_reference_fixtures(gpu_lib):
+    gold = np.load(G.os.path.join(G.HERE, "combos.npz"))
+    for n, c in enumerate(G.combo_list()):
+        s = gpu_sim(reference_params(**G.COMBO_BASE, **c))
+        s.set_prim(gold["q0"])
+        for k in range(3):
+            dt = s.compute_dt()[0]
+            assert bits_equal(dt, gold["dts"][n][k]), (c, k, dt, gold["dts"][n][k])
+            s.update(dt)
+        assert bits_equal(s.get_prim(), gold["q"][n]), c
+        s.close()
+
+
+def test_problems_match_reference_fixtures(gpu_lib):
+    gold = np.load(G.os.path.join(G.HERE, "problems.npz"))
+    for n, name in enumerate(G.PROBLEM_NAMES):
+        s = gpu_sim(reference_params(**G.PROBLEM_BASE))
+        s.init_problem(name)
+        for k in range(4):
+            dt = s.compute_dt()[0]
+            assert bits_equal(dt, gold["dts"][n][k]), name
+            s.update(dt)
+        assert bits_equal(s.get_prim(), gold["q"][n]), name
+        s.close()
+
+
+def test_sod_512x8_device_loop_matches_reference(gpu_lib):
+    """BASELINE Sod set-up run to t = 0.2 by the device-driven loop: the dt
+    sequence (per-iteration log) and the final primitives are the reference's."""
+    gold = np.load(G.os.path.join(G.HERE, "sod_512x8.npz"))
+    p = G.sod_params()
+    s = gpu_sim(p)
+    s.init_problem("sod_x")
+    t, n, status = s.advance(100000, p.tend)
+    from fv2d_gb300 import RUN_DONE
+    assert status == RUN_DONE
+    assert n == len(gold["dts"])
+    log = s.step_log()
+    assert bits_equal(log[:, 1], gold["dts"])
+    assert t == float(gold["t"])
+    assert bits_equal(s.get_prim(), gold["q"])
+
+
+def test_sod_granular_calls_match_device_loop(gpu_lib):
+    p = G.sod_params()
+    a, b = gpu_sim(p), gpu_sim(p)
+    a.init_problem("sod_x")
+    b.init_problem("sod_x")
+    t = 0.0
+    for _ in range(50):
+        dt = a.compute_dt()[0]
+        a.update(dt)
+        t += dt
+    tb, n, _ = b.advance(50, 10.0)
+    assert n == 50 and tb == t
+    assert bits_equal(a.get_prim(), b.get_prim())
+    assert bits_equal(a.get_cons(), b.get_cons())
+
+
+@pytest.mark.parametrize("shape", [(17, 33), (40, 65), (37, 100), (5, 3)])
+def test_odd_sizes_match_oracle(gpu_lib, shape):
+    ny, nx = shape
+    q0 = random_prim(ny, nx, 11 + nx)
+    for c in G.combo_list()[::7]:
+        p = reference_params(Nx=nx, Ny=ny, gamma0=1.4, CFL=0.6, **c)
+        o, s = Oracle(p), gpu_sim(p)
+        o.set_prim(q0)
+        s.set_prim(q0)
+        for _ in range(3):
+            d = o.compute_dt()
+            assert bits_equal(s.compute_dt()[0], d[0]), c
+            o.update(d[0])
+            s.update(d[0])
+        assert bits_equal(s.get_prim(), o.get_prim()), c
+        assert bits_equal(s.get_cons(), o.get_cons()), c
+        s.close()
+
+
+def test_muscl_hancock_extension_matches_oracle(gpu_lib):
+    q0 = random_prim(19, 37, 5, smooth=True)
+    for rs in (0, 1, 2):
+        for bc in (0, 1, 2):
+            p = reference_params(Nx=37, Ny=19, gamma0=1.4, CFL=0.5, reconstruction=3, riemann_solver=rs,
+                                 boundary_x=bc, boundary_y=(bc + 1) % 3)
+            o, s = Oracle(p), gpu_sim(p)
+            o.set_prim(q0)
+            s.set_prim(q0)
+            for _ in range(4):
+                d = o.compute_dt()
+                o.update(d[0])
+                s.update(d[0])
+            assert bits_equal(s.get_prim(), o.get_prim()), (rs, bc)
+            s.close()
+
+
+@pytest.mark.parametrize("name", ["sedov", "kh_step", "rt_hydrostatic", "H84", "C91", "gresho_vortex", "blast"])
+def test_initial_conditions_match_oracle(gpu_lib, name):
+    kw = dict(Nx=48, Ny=40, gamma0=1.4, CFL=0.5, reconstruction=2)
+    if name == "rt_hydrostatic":
+        kw.update(gravity_mode=1, gy=-0.1, riemann_solver=0, boundary_x=2, xmax=0.5, ymax=1.5)
+    if name in ("H84", "C91"):
+        kw.update(ymin=1.0, ymax=2.0, gravity_mode=1, gy=-1.0)
+    p = reference_params(**kw)
+    o, s = Oracle(p), gpu_sim(p)
+    o.init_problem(name)
+    s.init_problem(name)
+    assert bits_equal(s.get_prim(), o.get_prim())
+    for _ in range(3):
+        d = o.compute_dt()
+        assert bits_equal(s.compute_dt()[0], d[0])
+        o.update(d[0])
+        s.update(d[0])
+    assert bits_equal(s.get_prim(), o.get_prim())
+
+
+def test_negative_counters_match_oracle(gpu_lib):
+    p, q = negative_case()
+    o, s = Oracle(p), gpu_sim(p)
+    o.set_prim(q)
+    s.set_prim(q)
+    dt = o.compute_dt()[0]
+    o.update(2 * dt)
+    s.update(2 * dt)
+    assert s.counters() == o.counters() == [12, 0, 0]
+    assert bits_equal(s.get_prim(), o.get_prim())
+
+
+def test_device_loop_stops_for_snapshots(gpu_lib):
+    """main.cpp:62-84: the save test happens before dt at each iteration and
+    at most once per iteration."""
+    p = G.sod_params()
+    p.tend = 0.05
+    s = gpu_sim(p)
+    s.init_problem("sod_x")
+    o = Oracle(p)
+    o.init_problem("sod_x")
+    save_freq, next_save, t, ite = 0.01, 0.0, 0.0, 0
+    saves_host = []
+    while t + p.epsilon < p.tend:  # reference loop on the oracle
+        if t + p.epsilon > next_save:
+            saves_host.append(t)
+            next_save += save_freq
+        d = o.compute_dt()
+        o.update(d[0])
+        t += d[0]
+        ite += 1
+    saves_dev, next_save, skip = [], 0.0, False
+    while True:
+        td, n, status = s.advance(1000000, p.tend, next_save, skip)
+        from fv2d_gb300 import RUN_DONE, RUN_SAVE
+        if status == RUN_SAVE:
+            saves_dev.append(td)
+            next_save += save_freq
+            skip = True
+            continue
+        assert status == RUN_DONE
+        break
+    assert saves_dev == saves_host
+    assert td == t
+    assert bits_equal(s.get_prim(), o.get_prim())
+
+
+@pytest.mark.slow
+def test_full_size_sedov_matches_oracle(gpu_lib):
+    """Sedov 2048^2 (the benchmark grid): bitwise against the OpenMP oracle
+    for 3 iterations, then conservation and determinism over 40 more."""
+    p = reference_params(Nx=2048, Ny=2048, gamma0=1.4, reconstruction=2, riemann_solver=1, CFL=0.8,
+                         boundary_x=1, boundary_y=1)
+    o, s = Oracle(p), gpu_sim(p)
+    o.init_problem("sedov")
+    s.init_problem("sedov")
+    for _ in range(3):
+        d = o.compute_dt()
+        assert bits_equal(s.compute_dt()[0], d[0])
+        o.update(d[0])
+        s.update(d[0])
+    assert bits_equal(s.get_prim(), o.get_prim())
+    del o
+    u0 = s.get_cons()
+    s.advance(40, 1e9)
+    u1 = s.get_cons()
+    # reflecting walls: mass and energy are conserved to summation rounding
+    for k in (0, 3):
+        a, b = np.sum(u0[..., k], dtype=np.float64), np.sum(u1[..., k], dtype=np.float64)
+        assert abs(b - a) <= 1e-11 * abs(a), k
+    # run-to-run determinism
+    s2 = gpu_sim(p)
+    s2.init_problem("sedov")
+    for _ in range(3):
+        s2.update(s2.compute_dt()[0])
+    s2.advance(40, 1e9)
+    assert bits_equal(s2.get_cons(), u1)

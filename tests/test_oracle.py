@@ -1,0 +1,126 @@
+"""The CPU oracle against the reference's published known answer, the
+committed golden fixtures (produced by the reference's own headers) and,
+where the reference checkout was available at build time, the reference
+headers directly."""
+import numpy as np
+import pytest
+
+from fv2d_testlib import (Oracle, RefSim, bits_equal, random_prim, ref_available, reference_params)
+import golden.make_golden as G
+
+
+def test_readme_blast_dt_log():
+    """README.md:86-89: blast.ini prints dt_hyp 0.000521995 at t=0, then
+    0.000480941 and 0.000459815 after 11 and 22 iterations."""
+    p = reference_params(Nx=256, Ny=256, boundary_x=2, boundary_y=2, riemann_solver=1, reconstruction=0,
+                         CFL=0.1, gamma0=1.4, tend=1.0)
+    o = Oracle(p)
+    o.init_problem("blast")
+    hyp, dts = [], []
+    t = 0.0
+    for it in range(23):
+        d = o.compute_dt()
+        hyp.append(1.0 / d[1])
+        dts.append(d[0])
+        if it == 11:
+            assert f"{t:.6g}" == "0.000551063"
+        if it == 22:
+            assert f"{t:.6g}" == "0.00106851"
+        o.update(d[0])
+        t += d[0]
+    assert f"{hyp[0]:.6g}" == "0.000521995"
+    assert f"{hyp[11]:.6g}" == "0.000480941"
+    assert f"{hyp[22]:.6g}" == "0.000459815"
+    gold = np.load(G.os.path.join(G.HERE, "blast_readme.npz"))
+    assert bits_equal(np.array(dts), gold["dts"])
+
+
+def test_sod_golden():
+    gold = np.load(G.os.path.join(G.HERE, "sod_512x8.npz"))
+    p = G.sod_params()
+    o = Oracle(p)
+    o.init_problem("sod_x")
+    t, dts = o.run(p.tend, 100000)
+    assert len(dts) == len(gold["dts"])
+    assert bits_equal(dts, gold["dts"])
+    assert bits_equal(o.get_prim(), gold["q"])
+    assert t == float(gold["t"])
+
+
+def test_combos_golden():
+    gold = np.load(G.os.path.join(G.HERE, "combos.npz"))
+    for n, c in enumerate(G.combo_list()):
+        o = Oracle(reference_params(**G.COMBO_BASE, **c))
+        o.set_prim(gold["q0"])
+        for s in range(3):
+            d = o.compute_dt()
+            assert bits_equal(d[0], gold["dts"][n][s]), c
+            o.update(d[0])
+        assert bits_equal(o.get_prim(), gold["q"][n]), c
+
+
+def test_problems_golden():
+    gold = np.load(G.os.path.join(G.HERE, "problems.npz"))
+    for n, name in enumerate(G.PROBLEM_NAMES):
+        o = Oracle(reference_params(**G.PROBLEM_BASE))
+        o.init_problem(name)
+        for s in range(4):
+            d = o.compute_dt()
+            assert bits_equal(d[0], gold["dts"][n][s]), name
+            o.update(d[0])
+        assert bits_equal(o.get_prim(), gold["q"][n]), name
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference cross-check build (oracle/_ref) not present")
+@pytest.mark.parametrize("seed", [3, 4])
+def test_against_reference_headers(seed):
+    """Random states, odd sizes, every combination, 4 iterations."""
+    q0 = random_prim(9, 7, seed)
+    for c in G.combo_list()[::5]:
+        p = reference_params(Nx=7, Ny=9, gamma0=1.4, CFL=0.6, **c)
+        o, r = Oracle(p), RefSim(p)
+        o.set_prim(q0)
+        r.set_prim(q0)
+        for _ in range(4):
+            d = o.compute_dt()
+            dr = r.compute_dt()
+            assert bits_equal(d[0], dr), c
+            o.update(d[0])
+            r.update(dr)
+        assert bits_equal(o.get_prim(), r.get_prim()), c
+        assert bits_equal(o.get_cons(), r.get_cons()), c
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference cross-check build (oracle/_ref) not present")
+def test_reference_reads_floats():
+    """The reference's ini reader returns float-rounded reals (GetFloat)."""
+    p = reference_params(Nx=8, Ny=8, gamma0=1.4, CFL=0.8)
+    r = RefSim(p)
+    assert r.param("gamma0") == float(np.float32(1.4))
+    assert r.param("CFL") == float(np.float32(0.8))
+    assert r.param("epsilon") == float(np.float32(1e-6))
+
+
+def negative_case():
+    """A strong two-sided expansion advanced with twice the CFL step: the
+    update drives the central densities negative (used by the GPU tests too)."""
+    q = np.ones((6, 6, 4))
+    q[..., 2] = 0.0
+    q[..., 3] = 1e-3
+    q[:, :3, 1] = -30.0
+    q[:, 3:, 1] = 30.0
+    p = reference_params(Nx=6, Ny=6, gamma0=1.4, CFL=0.9, boundary_x=1, boundary_y=1)
+    return p, q
+
+
+def test_negative_reset_counters():
+    """checkNegatives (SimInfo.h:602-646): negative densities are reset to
+    epsilon_reset_negative and counted."""
+    p, q = negative_case()
+    o = Oracle(p)
+    o.set_prim(q)
+    d = o.compute_dt()
+    o.update(2.0 * d[0])
+    c = o.counters()
+    assert c[0] == 12 and c[2] == 0
+    assert (o.get_prim()[..., 0] > 0).all()
