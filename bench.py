@@ -1,0 +1,344 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 explicit hydro step (plain FP64 path).
+
+Workload (headline configuration): Sedov blast, 2048 x 2048 cells on
+[0,1]^2, rho = 1, u = v = 0, ambient p = 1e-5, E0 = 1 deposited as uniform
+pressure in the cells within r0 = 0.02 of the centre, gamma = 1.4, PLM/minmod,
+HLLC, CFL 0.8, reflecting walls, binary64.  Parameters are float-rounded the
+way the reference's .ini reader returns them.  One bench step is one full
+hydro iteration over the grid (dt reduction + fused update), computed on the
+device from the previous state.
+
+  value   cell-updates/s with the state resident in HBM: K iterations queued
+          with fv2d_run_async, timed with CUDA events on the library's stream
+          (the state, 402 MB, is larger than the 129 MB L2, so no flush).
+  e2e     the same metric through the C-ABI with host buffers: per step
+          fv2d_set_prim from page-locked host memory, fv2d_compute_dt,
+          fv2d_update, fv2d_get_prim into page-locked host memory.
+
+`--impl reference` times the reference algorithm on the host cores: the
+CPU oracle (an OpenMP restatement of the reference's pass structure, bit-exact
+with the reference's headers), on the same workload.
+
+Launched as `python bench.py --gpus N --steps K --warmup W` (N = 1) or under
+torch.distributed.run for N > 1: ranks run independent replicas (the step
+has no exchange between simulations) and `value` sums them.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+NX = NY = 2048
+BYTES_PER_CELL = 64  # read + write 4 x binary64 conservative state per cell-update
+METRIC = "cell-updates/s"
+WORKLOAD = "sedov_2048x2048_fp64_plain"
+
+
+def workload_params(fv, n):
+    f = fv.as_float32
+    return fv.default_params(Nx=n, Ny=n, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0, gamma0=f(1.4), CFL=f(0.8),
+                             reconstruction=fv.PLM, riemann_solver=fv.HLLC, boundary_x=fv.BC_REFLECTING,
+                             boundary_y=fv.BC_REFLECTING, time_stepping=fv.TS_EULER)
+
+
+def config(n, steps):
+    return {"workload": WORKLOAD, "grid": [n, n], "problem": "sedov", "scheme": "PLM-minmod + HLLC, Euler",
+            "cfl": 0.8, "gamma": 1.4, "boundaries": "reflecting", "steps": steps,
+            "l2": "state 402 MB (> 129 MB L2) streamed every step; no flush needed",
+            "precision": "binary64, bit-identical to the reference"}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_figures():
+    """Per-cell figures of the step kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "step_fp64_plm_hllc_sedov.txt")
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            if ":" in line and line.split(":", 1)[0].strip() in (
+                    "dram_bytes_per_cell", "fp64_flops_per_cell", "dram_bytes_per_launch_2048"):
+                k, v = line.split(":", 1)
+                try:
+                    out[k.strip()] = float(v.split()[0])
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = os.path.join("/tmp", f"fv2d_clocks_{os.getpid()}.csv")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(gpu_index), "-lms", "200"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_oracle_rate(n, steps_cap=20, budget_s=15.0):
+    """Oracle (OpenMP over all host cores) cell-updates/s on a bounded sample
+    of the workload: the same Sedov grid, as many iterations as fit ~budget."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import fv2d_testlib as T
+    lib = T.oracle_lib()
+    ncores = os.cpu_count() or 1
+    lib.fv2d_oracle_set_threads(ncores)
+    p = T.reference_params(Nx=n, Ny=n, gamma0=1.4, CFL=0.8, reconstruction=2, riemann_solver=1, boundary_x=1,
+                           boundary_y=1)
+    o = T.Oracle(p)
+    o.init_problem("sedov")
+    t0 = time.perf_counter()
+    d = o.compute_dt()
+    o.update(d[0])
+    one = time.perf_counter() - t0
+    steps = max(1, min(steps_cap, int(budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        d = o.compute_dt()
+        o.update(d[0])
+    el = time.perf_counter() - t0
+    return {"value": n * n * steps / el, "unit": METRIC, "cores": lib.fv2d_oracle_get_threads(), "kind": "port",
+            "sample": f"sedov {n}x{n}, {steps} iterations after 1 warm-up (oracle: OpenMP restatement of the "
+                      f"reference pass structure, -O3 -ffp-contract=off)", "seconds": el}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import fv2d_testlib as T
+    lib = T.oracle_lib()
+    ncores = os.cpu_count() or 1
+    lib.fv2d_oracle_set_threads(ncores)
+    p = T.reference_params(Nx=NX, Ny=NY, gamma0=1.4, CFL=0.8, reconstruction=2, riemann_solver=1, boundary_x=1,
+                           boundary_y=1)
+    o = T.Oracle(p)
+    o.init_problem("sedov")
+    for _ in range(args.warmup):
+        d = o.compute_dt()
+        o.update(d[0])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        d = o.compute_dt()
+        o.update(d[0])
+    el = time.perf_counter() - t0
+    v = NX * NY * args.steps / el
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Sedov initial condition)",
+            "config": config(NX, args.steps), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": lib.fv2d_oracle_get_threads(), "kind": "port",
+                             "sample": f"sedov {NX}x{NY}, {args.steps} iterations after {args.warmup} warm-up, "
+                                       "reference pass structure (the reference checkout and its Kokkos/HDF5 "
+                                       "dependencies are not available on this host)"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-4096", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    import fv2d_gb300 as fv
+    if not os.path.exists(fv.LIB_PATH):
+        from fv2d_gb300 import build as b
+        b.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    p = workload_params(fv, NX)
+    sim = fv.Simulation(p, device=local)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+
+    # warm-up on a first run, then restart from the initial condition so that
+    # the timed region is iterations 0..K-1 of the Sedov problem
+    sim.init_problem("sedov")
+    sim.run_async(args.warmup)
+    stream.synchronize()
+    sim.init_problem("sedov")
+    sim.set_time(0.0, 0)
+    stream.synchronize()
+
+    gpu_index = local
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if cvd:
+        ids = cvd.split(",")
+        if local < len(ids) and ids[local].strip().isdigit():
+            gpu_index = int(ids[local])
+    sampler = ClockSampler(gpu_index)
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    sim.run_async(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    t_sim, ite = sim.time()
+    if ite != args.steps:
+        raise RuntimeError(f"expected {args.steps} iterations, device reports {ite}")
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    cells = NX * NY
+    value = world * cells * args.steps / (ms_max * 1e-3)
+    ms_step = ms_max / args.steps
+
+    # roofline of the fused step kernel (one launch per iteration)
+    peak, peak_kind = measured_peaks()
+    achieved = BYTES_PER_CELL * cells / (ms_step * 1e-3) / 1e9
+    prof = profile_figures()
+    traffic = prof.get("dram_bytes_per_cell")
+    fp64_peak = fv.probe_fp64_peak(local)
+    fp64 = None
+    if "fp64_flops_per_cell" in prof:
+        ach = prof["fp64_flops_per_cell"] * cells / (ms_step * 1e-3) / 1e9
+        fp64 = {"achieved": ach, "peak": fp64_peak, "unit": "GFLOP/s", "frac": ach / fp64_peak,
+                "flops_per_cell": prof["fp64_flops_per_cell"], "peak_kind": "measured DFMA loop"}
+    else:
+        fp64 = {"achieved": None, "peak": fp64_peak, "unit": "GFLOP/s", "frac": None,
+                "peak_kind": "measured DFMA loop"}
+
+    # end to end through the C-ABI with host buffers
+    q0 = torch.empty((NY, NX, 4), dtype=torch.float64, pin_memory=True)
+    q1 = torch.empty_like(q0).pin_memory()
+    sim.init_problem("sedov")
+    sim.get_prim_ptr(q0.data_ptr())
+    ke = max(1, args.e2e_steps)
+    for _ in range(2):
+        sim.set_prim_ptr(q0.data_ptr())
+        sim.update(sim.compute_dt()[0])
+        sim.get_prim_ptr(q1.data_ptr())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        sim.set_prim_ptr(q0.data_ptr())
+        sim.update(sim.compute_dt()[0])
+        sim.get_prim_ptr(q1.data_ptr())
+    el = time.perf_counter() - t0
+    el_max = el
+    if dist is not None:
+        t = torch.tensor([el], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el_max = float(t.item())
+    e2e = {"value": world * cells * ke / el_max, "unit": METRIC, "h2d_bytes_per_step": cells * 32,
+           "d2h_bytes_per_step": cells * 32 + 8, "steps": ke,
+           "path": "fv2d_set_prim(pinned host) + fv2d_compute_dt + fv2d_update + fv2d_get_prim(pinned host)"}
+
+    extra = {}
+    if not args.no_4096 and world == 1:
+        p4 = workload_params(fv, 4096)
+        s4 = fv.Simulation(p4, device=local)
+        s4.set_stream(stream.cuda_stream)
+        s4.init_problem("sedov")
+        s4.run_async(5)
+        stream.synchronize()
+        k4 = max(10, args.steps // 10)
+        e0.record(stream)
+        s4.run_async(k4)
+        e1.record(stream)
+        e1.synchronize()
+        ms4 = e0.elapsed_time(e1) / k4
+        a4 = BYTES_PER_CELL * 4096 * 4096 / (ms4 * 1e-3) / 1e9
+        extra["sedov_4096"] = {"value": 4096 * 4096 / (ms4 * 1e-3), "unit": METRIC, "steps": k4,
+                               "ms_per_step": ms4, "hbm_achieved_gbs": a4, "hbm_frac": a4 / peak}
+        s4.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_oracle_rate(NX)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (Sedov initial condition, seeded inputs)",
+        "config": config(NX, args.steps),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": (traffic * cells) if traffic else None, "peak_kind": peak_kind,
+                     "bytes_per_cell": BYTES_PER_CELL, "kernel": "fv2d::step_kernel<PLM,HLLC>"},
+        "roofline_fp64": fp64,
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "gpu_launches": args.steps + 1,
+        "sim_time": t_sim,
+    }
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

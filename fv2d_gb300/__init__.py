@@ -66,6 +66,8 @@ def lib():
         L.fv2d_last_error.argtypes = [vp]
         L.fv2d_last_error.restype = C.c_char_p
         L.fv2d_build_info.argtypes = [C.c_char_p, C.c_int]
+        L.fv2d_run_async.argtypes = [vp, C.c_int]
+        L.fv2d_probe_fp64_peak.argtypes = [C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -83,6 +85,15 @@ def build_info():
     buf = C.create_string_buffer(256)
     lib().fv2d_build_info(buf, 256)
     return buf.value.decode()
+
+
+def probe_fp64_peak(device=0):
+    """Measured binary64 FMA throughput in GFLOP/s."""
+    g = C.c_double()
+    rc = lib().fv2d_probe_fp64_peak(device, C.byref(g))
+    if rc != 0:
+        raise Fv2dError(rc, "fp64 probe failed")
+    return g.value
 
 
 def _ptr(a):
@@ -182,6 +193,10 @@ class Simulation:
         if rc != 0 and s.value != RUN_NUMERIC:
             self._check(rc)
         return t.value, n.value, s.value
+
+    def run_async(self, n):
+        """Queue n device-driven iterations without synchronising."""
+        self._check(self._lib.fv2d_run_async(self.h, int(n)))
 
     def time(self):
         t = C.c_double()

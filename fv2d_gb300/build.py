@@ -40,6 +40,7 @@ UNITS = [
     ("step_hll.cu", ["-fmad=false"]),
     ("step_hllc.cu", ["-fmad=false"]),
     ("step_fslp.cu", ["-fmad=false"]),
+    ("probe.cu", []),
     ("problems.cpp", []),
 ]
 

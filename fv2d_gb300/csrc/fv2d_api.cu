@@ -351,6 +351,31 @@ int encode_maps(fv2d_ctx *ctx) {
   return FV2D_OK;
 }
 
+// Launch-bound loops are replayed from a CUDA graph of G fused steps; every
+// step reads its dt, buffer parity and stop flag from device memory, so one
+// captured sequence serves every replay and steps after a stop are no-ops.
+int ensure_graph(fv2d_ctx *ctx) {
+  const int G = 32;
+  if (ctx->graph && ctx->graph_stream == ctx->stream) return FV2D_OK;
+  if (ctx->graph) {
+    cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = FV2D_OK;
+  for (int k = 0; k < G && rc == FV2D_OK; ++k) rc = launch_update(ctx, 1, 0.0);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&ctx->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+  ctx->graph_stream = ctx->stream;
+  ctx->graph_steps = G;
+  return FV2D_OK;
+}
+
 void free_all(fv2d_ctx *c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (double *ptr : {c->Q[0], c->Q[1], c->U, c->U1, c->stage, c->kap_row, c->log})
@@ -591,28 +616,8 @@ int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, in
   begin_kernel<<<1, 1, 0, ctx->stream>>>(ctx->st, tend, next_save, ctx->p.epsilon, check_save,
                                          skip_first_save_check, max_steps);
   CK(cudaGetLastError());
-  // Launch-bound loops are replayed from a CUDA graph of G fused steps; every
-  // step reads its dt, buffer parity and stop flag from device memory, so one
-  // captured sequence serves every replay and steps after a stop are no-ops.
-  const int G = 32;
-  if (!ctx->graph || ctx->graph_stream != ctx->stream) {
-    if (ctx->graph) {
-      cudaGraphExecDestroy(ctx->graph);
-      ctx->graph = nullptr;
-    }
-    cudaGraph_t g;
-    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = FV2D_OK;
-    for (int k = 0; k < G && rc == FV2D_OK; ++k) rc = launch_update(ctx, 1, 0.0);
-    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-    if (rc) return rc;
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&ctx->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
-    ctx->graph_stream = ctx->stream;
-    ctx->graph_steps = G;
-  }
+  if (int rc = ensure_graph(ctx)) return rc;
+  const int G = ctx->graph_steps;
   int launched = 0;
   for (;;) {
     // keep a few replays in flight between status checks
@@ -634,6 +639,19 @@ int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, in
   if (status) *status = out;
   if (s.error) return fail(ctx, FV2D_ERR_CUDA, "a step kernel timed out waiting for its tile load");
   return out == FV2D_RUN_NUMERIC ? fail(ctx, FV2D_ERR_NUMERIC, "non-finite or non-positive dt") : FV2D_OK;
+}
+
+int fv2d_run_async(fv2d_ctx *ctx, int n) {
+  if (!ctx || n < 0) return FV2D_ERR_INVALID;
+  if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
+  begin_kernel<<<1, 1, 0, ctx->stream>>>(ctx->st, INFINITY, -1.0, ctx->p.epsilon, 0, 1, n);
+  CK(cudaGetLastError());
+  if (int rc = ensure_graph(ctx)) return rc;
+  int k = 0;
+  for (; k + ctx->graph_steps <= n; k += ctx->graph_steps) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+  for (; k < n; ++k)
+    if (int rc = launch_update(ctx, 1, 0.0)) return rc;
+  return FV2D_OK;
 }
 
 int fv2d_get_step_log(fv2d_ctx *ctx, double *records, int max_records, int *count) {

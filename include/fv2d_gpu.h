@@ -102,6 +102,14 @@ enum { FV2D_RUN_STEPS = 0, FV2D_RUN_DONE = 1, FV2D_RUN_SAVE = 2, FV2D_RUN_NUMERI
 int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, int skip_first_save_check,
                  double *t, int *steps_done, int *status);
 
+/* Queues n device-driven iterations on the context's stream and returns
+ * without synchronising: each iteration computes its dt on the device from
+ * the previous state (ComputeDt.h:18-65), updates (Update.h:193-222,
+ * SimInfo.h:576-646) and advances t (main.cpp:83).  No tend or snapshot stop;
+ * a non-finite or non-positive dt stops the remaining iterations.  Exactly n
+ * step launches (2n with RK2) plus one control launch are queued. */
+int fv2d_run_async(fv2d_ctx *ctx, int n);
+
 /* Simulation clock kept on the device (t after the last committed update,
  * iteration count).  set_time resets both (e.g. after a restart). */
 int fv2d_get_time(fv2d_ctx *ctx, double *t, int *iteration);
@@ -118,6 +126,11 @@ const char *fv2d_last_error(fv2d_ctx *ctx);
 /* Static description of the compiled kernels: writes a short text (tile
  * shape, threads per block, architecture) into buf. */
 int fv2d_build_info(char *buf, int len);
+
+/* Measured binary64 fused multiply-add throughput of `device` in GFLOP/s
+ * (2 flops per DFMA), from a dependent-chain-free DFMA loop timed with CUDA
+ * events.  Used to state the FP64 roofline of the step kernel. */
+int fv2d_probe_fp64_peak(int device, double *gflops);
 
 /* sizeof(fv2d_params) as compiled into the library. */
 size_t fv2d_params_size(void);
