@@ -13,7 +13,7 @@ import os
 import numpy as np
 
 from ._abi import (  # noqa: F401  (re-exported enums)
-    Params, PROBLEMS, ERROR_NAMES, as_float32,
+    Params, PROBLEMS, ERROR_NAMES, ERR_SIZE, as_float32,
     HLL, HLLC, FSLP, BC_ABSORBING, BC_REFLECTING, BC_PERIODIC, TS_EULER, TS_RK2,
     PCM, PCM_WB, PLM, MUSCL_HANCOCK, GRAV_NONE, GRAV_CONSTANT, GRAV_ANALYTICAL,
     BCTC_NONE, BCTC_FIXED_TEMPERATURE, BCTC_FIXED_GRADIENT, TCM_CONSTANT, TCM_B02,
@@ -68,6 +68,7 @@ def lib():
         L.fv2d_build_info.argtypes = [C.c_char_p, C.c_int]
         L.fv2d_run_async.argtypes = [vp, C.c_int]
         L.fv2d_probe_fp64_peak.argtypes = [C.c_int, _dp]
+        L.fv2d_compute_dt_noalloc.argtypes = [C.POINTER(Params), vp, vp, vp]
         _lib = L
     return _lib
 
@@ -94,6 +95,18 @@ def probe_fp64_peak(device=0):
     if rc != 0:
         raise Fv2dError(rc, "fp64 probe failed")
     return g.value
+
+
+NOALLOC_MAX_CELLS = 4096 * 4096
+
+
+def compute_dt_noalloc(params, q_dev_ptr, out_dev_ptr, stream_ptr=0):
+    """Allocation-free CFL dt of a device array of interleaved interior
+    primitives (for callers that cannot allocate device memory); writes
+    {dt, inv_dt_hyp, inv_dt_tc, inv_dt_visc} to the device array at
+    out_dev_ptr.  Returns the FV2D status code."""
+    return lib().fv2d_compute_dt_noalloc(C.byref(params), C.c_void_p(q_dev_ptr), C.c_void_p(out_dev_ptr),
+                                         C.c_void_p(stream_ptr))
 
 
 def _ptr(a):

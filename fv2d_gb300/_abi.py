@@ -97,8 +97,9 @@ PROBLEMS = {
     "sedov": 100, "kh_step": 101, "rt_hydrostatic": 102,
 }
 
-OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_NUMERIC, ERR_UNSUPPORTED = range(7)
-ERROR_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "NUMERIC", 6: "UNSUPPORTED"}
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_NUMERIC, ERR_UNSUPPORTED, ERR_SIZE = range(8)
+ERROR_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "NUMERIC", 6: "UNSUPPORTED",
+               7: "SIZE"}
 
 
 def as_float32(x):

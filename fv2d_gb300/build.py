@@ -41,6 +41,7 @@ UNITS = [
     ("step_hllc.cu", ["-fmad=false"]),
     ("step_fslp.cu", ["-fmad=false"]),
     ("probe.cu", []),
+    ("noalloc.cu", ["-fmad=false"]),
     ("problems.cpp", []),
 ]
 

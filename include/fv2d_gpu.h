@@ -132,6 +132,30 @@ int fv2d_build_info(char *buf, int len);
  * events.  Used to state the FP64 roofline of the step kernel. */
 int fv2d_probe_fp64_peak(int device, double *gflops);
 
+/* Allocation-free CFL time step.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc -- code whose device memory belongs
+ * to another allocator (a framework pool that must account for every byte, or
+ * a process that reserved all device memory up front) and loops that cannot
+ * afford the device-wide synchronisation an allocation may cause.
+ *
+ * Computes ComputeDtFunctor::computeDt (ComputeDt.h:18-65) of a caller-owned
+ * device array q_dev of interleaved interior primitives (Ny x Nx x
+ * {rho,u,v,p}, the layout of fv2d_set_prim_device) and writes
+ * {dt, inv_dt_hyp, inv_dt_tc, inv_dt_visc} to the caller-owned device array
+ * out_dev (4 doubles), queued on `stream` (a cudaStream_t, NULL = default
+ * stream); the result equals fv2d_compute_dt's on the same state bit for bit.
+ * It allocates nothing: its only scratch is a fixed array inside the library
+ * (32 KB + 256 B on every GPU that loads the library, held until exit), which
+ * limits the grid to FV2D_NOALLOC_MAX_CELLS cells; larger grids return
+ * FV2D_ERR_SIZE before any GPU work.  The first call on a device looks up the
+ * array's device address with that device current; make that first call
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU (other streams, other host threads) race -- serialise
+ * them. */
+#define FV2D_NOALLOC_CELLS_PER_BLOCK 4096
+#define FV2D_NOALLOC_MAX_CELLS (4096 * 4096)
+int fv2d_compute_dt_noalloc(const fv2d_params *p, const double *q_dev, double *out_dev, void *stream);
+
 /* sizeof(fv2d_params) as compiled into the library. */
 size_t fv2d_params_size(void);
 

@@ -88,7 +88,8 @@ enum {
   FV2D_ERR_NOMEM = 3,      /* device or host allocation failed */
   FV2D_ERR_STATE = 4,      /* call out of order (e.g. update before set_prim) */
   FV2D_ERR_NUMERIC = 5,    /* NaN or non-positive dt detected by the device guard */
-  FV2D_ERR_UNSUPPORTED = 6 /* valid in the reference but not provided here */
+  FV2D_ERR_UNSUPPORTED = 6, /* valid in the reference but not provided here */
+  FV2D_ERR_SIZE = 7         /* input larger than a fixed-size limit of the entry point */
 };
 
 /* The full parameter block.  Fill with fv2d_params_default() and override.
