@@ -32,6 +32,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
@@ -146,6 +148,88 @@ def cpu_oracle_rate(n, steps_cap=20, budget_s=15.0):
                       f"reference pass structure, -O3 -ffp-contract=off)", "seconds": el}
 
 
+def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, device=0):
+    """The batched FP32 service on the seeded request stream: requests are
+    submitted at their Poisson arrival times; every 16th request is also run
+    alone through the plain FP64 path (bit-identical to the reference) for
+    the time-to-solution and throughput comparison and the accuracy check."""
+    from fv2d_gb300.serve import Server, stream_requests, config_name
+    reqs = stream_requests(n=n_requests, rate=rate)
+    sample = set(range(0, len(reqs), sample_every))
+    srv = Server(budget_bytes=budget, device=device, autotune=True)
+    st0 = srv.stats()
+    results, ids, keep = {}, {}, {}
+    t_start = time.perf_counter()
+    k = 0
+    while k < len(reqs) or len(results) < len(reqs):
+        now = time.perf_counter() - t_start
+        while k < len(reqs) and reqs[k]["arrival"] <= now:
+            r = reqs[k]
+            ids[srv.submit(r["problem"], r["params"], r["steps"], lowmach=r["lowmach"])] = k
+            k += 1
+        for res in srv.poll():
+            i = ids[res.id]
+            results[i] = res
+            if i in sample:
+                keep[i] = srv.get_prim(res.id)
+            srv.release(res.id)
+        if k < len(reqs):
+            time.sleep(max(0.0, min(0.002, reqs[k]["arrival"] - (time.perf_counter() - t_start))))
+        else:
+            time.sleep(0.0005)
+    wall = time.perf_counter() - t_start
+    st = srv.stats()
+    cfgs = [config_name(st.bucket_cfg[b]) for b in range(4)]
+    srv.close()
+    tts = np.array([results[i].done_s - results[i].submit_s for i in range(len(reqs))])
+    work = sum(float(r["N"]) ** 2 * results[i].steps for i, r in enumerate(reqs))
+    first = min(results[i].submit_s for i in results)
+    last = max(results[i].done_s for i in results)
+    agg = work / (last - first)
+    # plain FP64 path, one request at a time, on the sample
+    sub = sorted(sample)
+    s_work, s_time, err_rho, err_p, drift, service = 0.0, 0.0, [], [], [], []
+    for i in sub:
+        r = reqs[i]
+        t0 = time.perf_counter()
+        sim = fv.Simulation(r["params"], device=device)
+        sim.init_problem(r["problem"])
+        sim.advance(r["steps"], 1e30)
+        q64 = sim.get_prim()
+        el = time.perf_counter() - t0
+        sim.close()
+        service.append(el)
+        s_work += float(r["N"]) ** 2 * r["steps"]
+        s_time += el
+        q32 = keep[i]
+        err_rho.append(float(np.sum(np.abs(q32[..., 0] - q64[..., 0])) / np.sum(np.abs(q64[..., 0]))))
+        err_p.append(float(np.sum(np.abs(q32[..., 3] - q64[..., 3])) / np.sum(np.abs(q64[..., 3]))))
+        res = results[i]
+        if r["kind"] != "sod":  # closed domains
+            drift.append(abs(res.cons1[0] - res.cons0[0]) / abs(res.cons0[0]))
+    plain_rate = s_work / s_time
+    # FIFO single-server queueing of the sample through the plain path
+    clock, tts64 = 0.0, []
+    for i, sv in zip(sub, service):
+        start = max(clock, reqs[i]["arrival"])
+        clock = start + sv
+        tts64.append(clock - reqs[i]["arrival"])
+    return {
+        "requests": len(reqs), "arrival_rate_hz": rate, "aggregate": agg, "unit": METRIC, "dtype": "f32 state/flux, "
+        "f64 clock/dt/conservation sums/low-Mach energy recovery", "wall_s": wall, "cell_updates": work,
+        "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
+        "tile_configs_per_bucket": cfgs, "replays": st.replays, "arena_reserved_gb": st.bytes_reserved / 1e9,
+        "plain_fp64_one_at_a_time": {"sample": len(sub), "aggregate": plain_rate, "unit": METRIC,
+                                     "p50_s": float(np.percentile(tts64, 50)),
+                                     "p99_s": float(np.percentile(tts64, 99)),
+                                     "note": "every 16th request, FIFO single server at the same arrival times"},
+        "ratio_vs_plain_fp64": agg / plain_rate,
+        "accuracy_vs_fp64": {"l1_rho_max": max(err_rho), "l1_rho_median": float(np.median(err_rho)),
+                             "l1_p_max": max(err_p), "mass_drift_max": max(drift) if drift else None,
+                             "sample": len(sub)},
+    }
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -188,6 +272,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-4096", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-requests", type=int, default=512)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -317,6 +403,11 @@ def main():
                                "ms_per_step": ms4, "hbm_achieved_gbs": a4, "hbm_frac": a4 / peak}
         s4.close()
 
+    served = None
+    if world == 1 and not args.no_served:
+        import numpy  # noqa: F401
+        served = run_served(fv, n_requests=args.served_requests, device=local)
+
     if rank != 0:
         return
     cpu = None
@@ -334,6 +425,7 @@ def main():
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": args.steps + 1,
         "sim_time": t_sim,
+        "served": served,
     }
     line.update(extra)
     print(json.dumps(line), flush=True)

@@ -42,6 +42,8 @@ UNITS = [
     ("step_fslp.cu", ["-fmad=false"]),
     ("probe.cu", []),
     ("noalloc.cu", ["-fmad=false"]),
+    ("batch_kernels.cu", ["-use_fast_math"]),
+    ("serve.cu", []),
     ("problems.cpp", []),
 ]
 

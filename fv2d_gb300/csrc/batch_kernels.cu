@@ -1,0 +1,54 @@
+// batch_kernels.cu -- the tile configurations of the batched FP32 step that
+// the autotuner chooses from (tile shape, threads per CTA, halo staging).
+// Compiled with fast single-precision math: the service's tolerance is set
+// against the binary64 path, not bit parity.
+#include "batch_kernel.cuh"
+
+namespace fv2d {
+
+struct BatchCfg {
+  int tx, ty, nt, staging;
+  const char *name;
+  size_t smem;
+  const void *fn;
+};
+
+#define FV2D_CFG(TX, TY, NT, ST, NAME) \
+  {TX, TY, NT, ST, NAME, BatchSmem<TX, TY>::BYTES, (const void *)batch_step_kernel<TX, TY, NT, ST>}
+
+static const BatchCfg kCfgs[] = {
+    FV2D_CFG(32, 8, 128, 0, "32x8/128/ldg"),
+    FV2D_CFG(32, 16, 256, 0, "32x16/256/ldg"),
+    FV2D_CFG(32, 16, 256, 1, "32x16/256/tma"),
+    FV2D_CFG(32, 32, 256, 1, "32x32/256/tma"),
+    FV2D_CFG(32, 32, 512, 0, "32x32/512/ldg"),
+    FV2D_CFG(64, 16, 256, 1, "64x16/256/tma"),
+};
+
+int batch_num_cfgs() { return (int)(sizeof(kCfgs) / sizeof(kCfgs[0])); }
+
+void batch_cfg_info(int i, int *tx, int *ty, int *nt, int *staging, size_t *smem, const char **name) {
+  const BatchCfg &c = kCfgs[i];
+  if (tx) *tx = c.tx;
+  if (ty) *ty = c.ty;
+  if (nt) *nt = c.nt;
+  if (staging) *staging = c.staging;
+  if (smem) *smem = c.smem;
+  if (name) *name = c.name;
+}
+
+// Sets the shared-memory limit and returns resident CTAs per SM.
+cudaError_t batch_setup(int i, int *ctas_per_sm) {
+  const BatchCfg &c = kCfgs[i];
+  cudaError_t e = cudaFuncSetAttribute(c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, c.fn, c.nt, c.smem);
+}
+
+cudaError_t batch_launch(int i, int grid, cudaStream_t s, const BatchArgs &a) {
+  const BatchCfg &c = kCfgs[i];
+  void *args[] = {(void *)&a};
+  return cudaLaunchKernel(c.fn, dim3(grid), dim3(c.nt), args, c.smem, s);
+}
+
+}  // namespace fv2d

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/fv2d_gpu.h"
+#include "ic.h"
 #include "problems.h"
 #include "step_common.cuh"
 #include "physics.cuh"

@@ -11,10 +11,8 @@ namespace fv2d {
 void params_default(fv2d_params *p);
 const char *validate(const fv2d_params &p);  // nullptr when valid
 bool problem_valid(int problem);
-void init_cell(const fv2d_params &p, int problem, int i, int j, double *q);
 float analytical_gravity_row(const fv2d_params &p, int j);
 void kappa_row(const fv2d_params &p, int j, double out[4]);
 void parabolic_inv_dt(const fv2d_params &p, double *inv_tc, double *inv_visc);
-double uniform01(int32_t seed, int64_t cell, int32_t stream);
 
 }  // namespace fv2d

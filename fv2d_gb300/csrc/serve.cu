@@ -1,0 +1,913 @@
+// serve.cu -- the batched FP32 service (include/fv2d_serve.h).
+//
+// Host side: a worker thread owns the GPU stream.  Between graph replays it
+//   1. admits queued requests while the HBM budget allows (state buffers come
+//      from a chunked arena, so admission does not call cudaMalloc once the
+//      arena has grown to the working-set size),
+//   2. initialises them on the device (initial condition in binary64 ->
+//      binary32 state with its ghost ring, first dt, conservation sums),
+//   3. rebuilds the per-bucket (simulation, tile) work lists,
+//   4. replays a CUDA graph of K steps (K sized to ~3 ms of work), where each
+//      step is one persistent-kernel launch per non-empty grid-size bucket,
+//   5. reads the simulation table back and retires finished simulations
+//      (final conservation sums, state copied to host memory, arena freed).
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/fv2d_serve.h"
+#include "batch_common.cuh"
+#include "ic.h"
+#include "physics.cuh"
+#include "problems.h"
+
+namespace fv2d {
+int batch_num_cfgs();
+void batch_cfg_info(int i, int *tx, int *ty, int *nt, int *staging, size_t *smem, const char **name);
+cudaError_t batch_setup(int i, int *ctas_per_sm);
+cudaError_t batch_launch(int i, int grid, cudaStream_t s, const BatchArgs &a);
+}  // namespace fv2d
+
+using namespace fv2d;
+
+namespace {
+
+constexpr int kBuckets = 4;
+constexpr int kConsBlocks = 64;
+
+int bucket_of(int N) { return N < 128 ? 0 : (N < 256 ? 1 : (N < 512 ? 2 : 3)); }
+
+// ---------------------------------------------------------------- kernels
+// Initial state of one simulation: every padded cell (ghosts included) takes
+// the binary64 initial condition of its source cell (BoundaryConditions.h
+// maps), converted to conservative variables and stored in binary32.
+__global__ void ic_kernel(fv2d_params p, int problem, float *U, long long plane, int pitch, int N) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int W = N + 4;
+  if (idx >= (long long)W * W) return;
+  const int py = (int)(idx / W), px = (int)(idx % W);
+  int sx = px - 2, sy = py - 2;
+  bool nx = false, ny = false;
+  if (sx < 0 || sx >= N) sx = ghost_source(sx, N, p.boundary_x, &nx);
+  if (sy < 0 || sy >= N) sy = ghost_source(sy, N, p.boundary_y, &ny);
+  double q[4];
+  init_cell(p, problem, sx, sy, q);
+  if (nx) q[1] = -q[1];
+  if (ny) q[2] = -q[2];
+  const Gas<double> g{p.gamma0, p.gamma0 - 1.0, 1.0 / (p.gamma0 - 1.0), 0.0};
+  const S4<double> u = prim_to_cons(S4<double>{q[0], q[1], q[2], q[3]}, g);
+  const long long o = (long long)py * pitch + px;
+  U[o] = (float)u.r;
+  U[plane + o] = (float)u.u;
+  U[2 * plane + o] = (float)u.v;
+  U[3 * plane + o] = (float)u.p;
+}
+
+// Inverse hyperbolic dt of the current state of simulation `slot` (same
+// per-cell expression as the step epilogue), max into acc_bits.
+__global__ void first_dt_kernel(SimDev *sims, int slot) {
+  const SimDev &S = sims[slot];
+  const int N = S.N;
+  const float *U = S.U[S.cur];
+  float m = 0.f;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < (long long)N * N;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(c / N), i = (int)(c % N);
+    const long long g = (long long)(j + 2) * S.pitch + (i + 2);
+    float r = U[g], u = U[S.plane + g] / r, v = U[2 * S.plane + g] / r;
+    float p = (U[3 * S.plane + g] - 0.5f * r * (u * u + v * v)) * S.gm1;
+    if (S.lowmach)
+      p = (float)(((double)U[3 * S.plane + g] - 0.5 * (double)r * ((double)u * u + (double)v * v)) * (double)S.gm1);
+    if (r < 0.f) r = 1e-8f;
+    if (p < 0.f) p = 1e-8f;
+    const float cs = sqrtf(p * S.gamma / r);
+    const float ih = (cs + fabsf(u)) * S.inv_dx + (cs + fabsf(v)) * S.inv_dy;
+    if (ih > m) m = ih;
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(&sims[slot].acc_bits, __float_as_uint(m));
+}
+
+__global__ void first_dt_finish(SimDev *sims, int slot) {
+  SimDev &S = sims[slot];
+  double m = (double)__uint_as_float(S.acc_bits);
+  if (m < S.inv_tc) m = S.inv_tc;
+  if (m < S.inv_visc) m = S.inv_visc;
+  S.dt = S.cfl / m;
+  S.acc_bits = 0u;
+  if (!(S.dt > 0.0) || isinf(S.dt)) S.status = SIM_FAILED;
+  if (S.max_steps <= 0 || !(S.t + S.eps < S.tend)) S.status = SIM_DONE;
+}
+
+// Compensated (Neumaier) binary64 partial sums of the four conserved fields
+// of simulation `slot`; out[block][field][sum, compensation].
+__device__ __forceinline__ void neumaier_add(double &s, double &c, double x) {
+  const double t = s + x;
+  c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+  s = t;
+}
+__global__ void __launch_bounds__(256) cons_kernel(const SimDev *sims, int slot, double *out) {
+  const SimDev &S = sims[slot];
+  const int N = S.N;
+  const float *U = S.U[S.cur];
+  double s[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < (long long)N * N;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(k / N), i = (int)(k % N);
+    const long long g = (long long)(j + 2) * S.pitch + (i + 2);
+    for (int f = 0; f < 4; ++f) neumaier_add(s[f], c[f], (double)U[f * S.plane + g]);
+  }
+  __shared__ double sh[8][256];
+  for (int f = 0; f < 4; ++f) {
+    sh[2 * f][threadIdx.x] = s[f];
+    sh[2 * f + 1][threadIdx.x] = c[f];
+  }
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    const int f = threadIdx.x >> 1, comp = threadIdx.x & 1;
+    if (comp == 0) {
+      double ss = 0, cc = 0;
+      for (int t = 0; t < 256; ++t) {
+        neumaier_add(ss, cc, sh[2 * f][t]);
+        cc += sh[2 * f + 1][t];
+      }
+      out[(blockIdx.x * 4 + f) * 2] = ss;
+      out[(blockIdx.x * 4 + f) * 2 + 1] = cc;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- arena
+struct Arena {
+  struct Chunk {
+    char *base;
+    size_t size;
+    std::map<size_t, size_t> free;  // offset -> size
+  };
+  std::vector<Chunk> chunks;
+  double budget = 0;
+  size_t reserved = 0, in_use = 0;
+
+  static size_t align(size_t n) { return (n + 255) & ~size_t(255); }
+
+  void *alloc(size_t n) {
+    n = align(n);
+    for (auto &c : chunks)
+      for (auto it = c.free.begin(); it != c.free.end(); ++it)
+        if (it->second >= n) {
+          const size_t off = it->first, sz = it->second;
+          c.free.erase(it);
+          if (sz > n) c.free[off + n] = sz - n;
+          in_use += n;
+          return c.base + off;
+        }
+    // grow: chunks of at least 1 GiB, within the budget
+    size_t want = std::max(n, (size_t)1 << 30);
+    if ((double)(reserved + want) > budget) want = n;
+    if ((double)(reserved + want) > budget) return nullptr;
+    char *p = nullptr;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    Chunk c{p, want, {}};
+    if (want > n) c.free[n] = want - n;
+    chunks.push_back(std::move(c));
+    reserved += want;
+    in_use += n;
+    return p;
+  }
+  void release(void *ptr, size_t n) {
+    n = align(n);
+    char *p = static_cast<char *>(ptr);
+    for (auto &c : chunks)
+      if (p >= c.base && p < c.base + c.size) {
+        const size_t off = p - c.base;
+        in_use -= n;
+        auto next = c.free.lower_bound(off);
+        if (next != c.free.end() && next->first == off + n) {  // merge with the following block
+          n += next->second;
+          next = c.free.erase(next);
+        }
+        if (next != c.free.begin()) {  // merge with the preceding block
+          auto prev = std::prev(next);
+          if (prev->first + prev->second == off) {
+            prev->second += n;
+            return;
+          }
+        }
+        c.free[off] = n;
+        return;
+      }
+  }
+  void free_all() {
+    for (auto &c : chunks) cudaFree(c.base);
+    chunks.clear();
+    reserved = in_use = 0;
+  }
+};
+
+struct Pending {
+  int64_t id;
+  fv2d_request req;
+  double submit_s;
+};
+
+struct Slot {
+  bool used = false;
+  int64_t id = -1;
+  fv2d_request req;
+  int bucket = 0, cfg = 0;
+  void *mem = nullptr;
+  size_t bytes = 0;
+  double submit_s = 0, admit_s = 0;
+  double cons0[4] = {0, 0, 0, 0};
+  double cells_done = 0;
+  int steps_seen = 0;
+};
+
+struct Finished {
+  fv2d_result res;
+  std::vector<float> U;  // interior conservative planes, N x N each
+  double gamma;
+};
+
+}  // namespace
+
+struct fv2d_server {
+  fv2d_server_config cfg;
+  int device = 0, num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::chrono::steady_clock::time_point t0;
+  // simulation table
+  int max_sims = 0;
+  SimDev *d_sims = nullptr;
+  SimDev *h_up = nullptr, *h_down = nullptr;  // pinned mirrors (uploads / readbacks)
+  CUtensorMap *d_tmaps = nullptr, *h_tmaps = nullptr;
+  std::vector<Slot> slots;
+  std::vector<int> free_slots;
+  // per-bucket work lists
+  WorkItem *d_work[kBuckets] = {};
+  int *d_nwork = nullptr, *h_nwork = nullptr;
+  WorkItem *h_work[kBuckets] = {};
+  int work_cap[kBuckets] = {};
+  int bucket_cfg[kBuckets] = {1, 2, 3, 3};
+  int cfg_grid[16] = {};
+  bool lists_dirty = true;
+  int mask = 0;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (K, bucket mask) -> graph
+  double *d_cons = nullptr, *h_cons = nullptr;
+  float *h_stage = nullptr;
+  size_t h_stage_size = 0;
+  Arena arena;
+  // queues
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Pending> queue;
+  std::vector<fv2d_result> done_unpolled;
+  std::unordered_map<int64_t, Finished> finished;
+  int64_t next_id = 1;
+  int64_t n_submitted = 0, n_admitted = 0, n_completed = 0, n_failed = 0;
+  std::atomic<bool> stop{false};
+  std::thread worker;
+  double cell_updates = 0, busy_s = 0;
+  int replays = 0;
+  double rate_est = 2e10;  // cell-updates/s, refined by measurement
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+
+  double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  }
+  return fn;
+}
+
+const char *check_request(const fv2d_request &r) {
+  const fv2d_params &p = r.params;
+  if (r.struct_size != sizeof(fv2d_request)) return "fv2d_request.struct_size mismatch";
+  if (const char *w = validate(p)) return w;
+  if (p.Nx != p.Ny) return "the service runs square grids (Nx == Ny)";
+  if (p.Nx % 32 != 0 || p.Nx < 64 || p.Nx > 4096) return "N must be a multiple of 32 in [64, 4096]";
+  if (!problem_valid(r.problem)) return "unknown problem";
+  if (p.reconstruction != FV2D_PCM && p.reconstruction != FV2D_PCM_WB && p.reconstruction != FV2D_PLM)
+    return "the service provides PCM and PLM reconstruction";
+  if (p.riemann_solver == FV2D_FSLP) return "the service provides HLL and HLLC";
+  if (p.time_stepping != FV2D_TS_EULER) return "the service provides Euler stepping";
+  if (p.gravity_mode == FV2D_GRAV_ANALYTICAL || p.well_balanced_flux_at_y_bc) return "constant gravity only";
+  if (p.thermal_conductivity_active && (p.thermal_conductivity_mode != FV2D_TCM_CONSTANT ||
+                                        p.bctc_ymin != FV2D_BCTC_NONE || p.bctc_ymax != FV2D_BCTC_NONE))
+    return "constant conductivity without boundary modes only";
+  if (r.max_steps < 0) return "max_steps < 0";
+  return nullptr;
+}
+
+size_t state_bytes(int N, int *pitch, long long *plane) {
+  *pitch = (N + 4 + 31) / 32 * 32;
+  *plane = (long long)(N + 4) * *pitch;
+  return sizeof(float) * 8 * (size_t)*plane;  // two buffers x four planes
+}
+
+// Admit one request into a free slot; returns the slot, or -1 when it does
+// not fit.
+int admit(fv2d_server *s, const Pending &pd) {
+  if (s->free_slots.empty()) return -1;
+  const fv2d_request &r = pd.req;
+  const fv2d_params &p = r.params;
+  const int N = p.Nx;
+  int pitch;
+  long long plane;
+  const size_t bytes = state_bytes(N, &pitch, &plane);
+  void *mem = s->arena.alloc(bytes);
+  if (!mem) return -1;
+  const int slot = s->free_slots.back();
+  s->free_slots.pop_back();
+  Slot &sl = s->slots[slot];
+  sl.used = true;
+  sl.id = pd.id;
+  sl.req = r;
+  sl.bucket = bucket_of(N);
+  sl.cfg = s->bucket_cfg[sl.bucket];
+  sl.mem = mem;
+  sl.bytes = bytes;
+  sl.submit_s = pd.submit_s;
+  sl.admit_s = s->now();
+  sl.cells_done = 0;
+  sl.steps_seen = 0;
+  int tx, ty, nt, staging;
+  batch_cfg_info(sl.cfg, &tx, &ty, &nt, &staging, nullptr, nullptr);
+
+  SimDev &d = s->h_up[slot];
+  std::memset(&d, 0, sizeof(d));
+  d.U[0] = static_cast<float *>(mem);
+  d.U[1] = static_cast<float *>(mem) + 4 * plane;
+  d.plane = plane;
+  d.pitch = pitch;
+  d.N = N;
+  d.ntx = (N + tx - 1) / tx;
+  d.nty = (N + ty - 1) / ty;
+  d.cur = 0;
+  d.status = SIM_ACTIVE;
+  d.step = 0;
+  d.max_steps = r.max_steps;
+  d.t = 0.0;
+  d.dt = 0.0;
+  d.tend = r.tend > 0 ? r.tend : INFINITY;
+  d.eps = p.epsilon;
+  parabolic_inv_dt(p, &d.inv_tc, &d.inv_visc);
+  d.cfl = p.CFL;
+  d.gamma = (float)p.gamma0;
+  d.gm1 = (float)(p.gamma0 - 1.0);
+  d.entho = (float)(1.0 / (p.gamma0 - 1.0));
+  const double dx = (p.xmax - p.xmin) / N, dy = (p.ymax - p.ymin) / N;
+  d.dx = (float)dx;
+  d.dy = (float)dy;
+  d.inv_dx = (float)(1.0 / dx);
+  d.inv_dy = (float)(1.0 / dy);
+  d.gx = (float)p.gx;
+  d.gy = (float)p.gy;
+  d.kappa = (float)p.kappa;
+  d.mu = (float)p.mu;
+  d.rs = p.riemann_solver == FV2D_HLL ? RS_HLL : RS_HLLC;
+  d.recon = p.reconstruction == FV2D_PLM ? 2 : 0;
+  d.bcx = p.boundary_x;
+  d.bcy = p.boundary_y;
+  d.grav = p.gravity_mode == FV2D_GRAV_CONSTANT;
+  d.tc = p.thermal_conductivity_active ? 1 : 0;
+  d.visc = p.viscosity_active ? 1 : 0;
+  d.lowmach = r.lowmach ? 1 : 0;
+  d.tma_ok = 0;
+  if (staging) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    bool ok = enc != nullptr;
+    for (int b = 0; b < 2 && ok; ++b) {
+      cuuint64_t dims[3] = {(cuuint64_t)(N + 4), (cuuint64_t)(N + 4), 4};
+      cuuint64_t strides[2] = {(cuuint64_t)pitch * 4, (cuuint64_t)plane * 4};
+      cuuint32_t box[3] = {(cuuint32_t)(tx + 4), (cuuint32_t)(ty + 4), 4};
+      cuuint32_t es[3] = {1, 1, 1};
+      ok = enc(&s->h_tmaps[2 * slot + b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, d.U[b], dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+    d.tma_ok = ok ? 1 : 0;
+    if (ok)
+      cudaMemcpyAsync(&s->d_tmaps[2 * slot], &s->h_tmaps[2 * slot], 2 * sizeof(CUtensorMap), cudaMemcpyHostToDevice,
+                      s->stream);
+  }
+  cudaMemcpyAsync(&s->d_sims[slot], &d, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream);
+  const long long W = N + 4;
+  ic_kernel<<<(unsigned)((W * W + 255) / 256), 256, 0, s->stream>>>(p, r.problem, d.U[0], plane, pitch, N);
+  const int nb = (int)std::min<long long>(1024, ((long long)N * N + 255) / 256);
+  first_dt_kernel<<<nb, 256, 0, s->stream>>>(s->d_sims, slot);
+  first_dt_finish<<<1, 1, 0, s->stream>>>(s->d_sims, slot);
+  cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
+  s->n_admitted++;
+  s->lists_dirty = true;
+  return slot;
+}
+
+void sum_cons(const double *part, double out[4]) {
+  for (int f = 0; f < 4; ++f) {
+    double ss = 0, cc = 0;
+    for (int b = 0; b < kConsBlocks; ++b) {
+      const double x = part[(b * 4 + f) * 2];
+      const double t = ss + x;
+      cc += (std::fabs(ss) >= std::fabs(x)) ? (ss - t) + x : (x - t) + ss;
+      ss = t;
+      cc += part[(b * 4 + f) * 2 + 1];
+    }
+    out[f] = ss + cc;
+  }
+}
+
+// Initial conservation sums of the slots admitted since the last replay.
+void read_initial_cons(fv2d_server *s, const std::vector<int> &fresh) {
+  if (fresh.empty()) return;
+  for (int slot : fresh)
+    cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
+                    sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
+  cudaStreamSynchronize(s->stream);
+  for (int slot : fresh) {
+    Slot &sl = s->slots[slot];
+    const fv2d_params &p = sl.req.params;
+    const double area = ((p.xmax - p.xmin) / p.Nx) * ((p.ymax - p.ymin) / p.Ny);
+    sum_cons(s->h_cons + (size_t)slot * kConsBlocks * 8, sl.cons0);
+    for (int f = 0; f < 4; ++f) sl.cons0[f] *= area;
+  }
+}
+
+void rebuild_lists(fv2d_server *s) {
+  std::vector<WorkItem> lists[kBuckets];
+  // interleave tiles of the simulations of a bucket so that a CTA's
+  // consecutive items belong to different simulations
+  std::vector<int> per_bucket[kBuckets];
+  for (int k = 0; k < s->max_sims; ++k)
+    if (s->slots[k].used) per_bucket[s->slots[k].bucket].push_back(k);
+  s->mask = 0;
+  for (int b = 0; b < kBuckets; ++b) {
+    for (int slot : per_bucket[b]) {
+      const SimDev &d = s->h_up[slot];
+      for (int ty = 0; ty < d.nty; ++ty)
+        for (int tx = 0; tx < d.ntx; ++tx) lists[b].push_back(WorkItem{slot, (short)tx, (short)ty});
+    }
+    if (!lists[b].empty()) s->mask |= 1 << b;
+    const int n = (int)lists[b].size();
+    if (n > s->work_cap[b]) {
+      int cap = std::max(1024, s->work_cap[b]);
+      while (cap < n) cap *= 2;
+      cudaStreamSynchronize(s->stream);
+      if (s->d_work[b]) cudaFree(s->d_work[b]);
+      if (s->h_work[b]) cudaFreeHost(s->h_work[b]);
+      cudaMalloc(&s->d_work[b], sizeof(WorkItem) * cap);
+      cudaMallocHost(&s->h_work[b], sizeof(WorkItem) * cap);
+      s->work_cap[b] = cap;
+      for (auto &g : s->graphs) cudaGraphExecDestroy(g.second);  // kernel arguments changed
+      s->graphs.clear();
+    }
+    s->h_nwork[b] = n;
+    if (n) {
+      std::memcpy(s->h_work[b], lists[b].data(), sizeof(WorkItem) * n);
+      cudaMemcpyAsync(s->d_work[b], s->h_work[b], sizeof(WorkItem) * n, cudaMemcpyHostToDevice, s->stream);
+    }
+  }
+  cudaMemcpyAsync(s->d_nwork, s->h_nwork, sizeof(int) * kBuckets, cudaMemcpyHostToDevice, s->stream);
+  s->lists_dirty = false;
+}
+
+cudaError_t launch_step(fv2d_server *s, int mask) {
+  for (int b = 0; b < kBuckets; ++b) {
+    if (!(mask & (1 << b))) continue;
+    BatchArgs a{s->d_sims, s->d_work[b], s->d_nwork + b, s->d_tmaps};
+    const int c = s->bucket_cfg[b];
+    cudaError_t e = batch_launch(c, s->cfg_grid[c], s->stream, a);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaGraphExec_t get_graph(fv2d_server *s, int K, int mask) {
+  auto key = std::make_pair(K, mask);
+  auto it = s->graphs.find(key);
+  if (it != s->graphs.end()) return it->second;
+  cudaGraph_t g;
+  if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
+  for (int k = 0; k < K; ++k) launch_step(s, mask);
+  if (cudaStreamEndCapture(s->stream, &g) != cudaSuccess) return nullptr;
+  cudaGraphExec_t ex = nullptr;
+  if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ex = nullptr;
+  cudaGraphDestroy(g);
+  if (ex) s->graphs[key] = ex;
+  return ex;
+}
+
+void retire(fv2d_server *s, int slot, const SimDev &d) {
+  Slot &sl = s->slots[slot];
+  const int N = d.N;
+  Finished fin;
+  fv2d_result &r = fin.res;
+  std::memset(&r, 0, sizeof(r));
+  r.id = sl.id;
+  r.status = d.status == SIM_DONE ? FV2D_OK : FV2D_ERR_NUMERIC;
+  r.steps = d.step;
+  r.t = d.t;
+  r.submit_s = sl.submit_s;
+  r.admit_s = sl.admit_s;
+  r.negatives = d.negatives;
+  r.N = N;
+  r.bucket = sl.bucket;
+  for (int f = 0; f < 4; ++f) r.cons0[f] = sl.cons0[f];
+  // final conservation sums and state
+  cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
+  cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
+                  sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
+  const size_t need = sizeof(float) * 4 * (size_t)N * N;
+  if (s->h_stage_size < need) {
+    if (s->h_stage) cudaFreeHost(s->h_stage);
+    cudaMallocHost(&s->h_stage, need);
+    s->h_stage_size = need;
+  }
+  for (int f = 0; f < 4; ++f)
+    cudaMemcpy2DAsync(s->h_stage + (size_t)f * N * N, sizeof(float) * N, d.U[d.cur] + f * d.plane + 2 * d.pitch + 2,
+                      sizeof(float) * d.pitch, sizeof(float) * N, N, cudaMemcpyDeviceToHost, s->stream);
+  cudaStreamSynchronize(s->stream);
+  double c1[4];
+  sum_cons(s->h_cons + (size_t)slot * kConsBlocks * 8, c1);
+  const fv2d_params &p = sl.req.params;
+  const double area = ((p.xmax - p.xmin) / p.Nx) * ((p.ymax - p.ymin) / p.Ny);
+  for (int f = 0; f < 4; ++f) r.cons1[f] = c1[f] * area;
+  fin.U.assign(s->h_stage, s->h_stage + 4 * (size_t)N * N);
+  fin.gamma = p.gamma0;
+  r.done_s = s->now();
+  s->arena.release(sl.mem, sl.bytes);
+  sl.used = false;
+  sl.mem = nullptr;
+  s->free_slots.push_back(slot);
+  s->lists_dirty = true;
+  // mark the device slot free so stale list entries are skipped
+  s->h_up[slot].status = SIM_FREE;
+  cudaMemcpyAsync(&s->d_sims[slot].status, &s->h_up[slot].status, sizeof(int), cudaMemcpyHostToDevice, s->stream);
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (r.status == FV2D_OK)
+    s->n_completed++;
+  else
+    s->n_failed++;
+  s->done_unpolled.push_back(r);
+  s->finished.emplace(r.id, std::move(fin));
+  s->cv.notify_all();
+}
+
+// Replay K steps of every active simulation and retire the finished ones.
+// Returns false when nothing was active.
+bool run_once(fv2d_server *s, int K_fixed) {
+  bool any = false;
+  double active_cells = 0;
+  for (int k = 0; k < s->max_sims; ++k)
+    if (s->slots[k].used) {
+      any = true;
+      active_cells += (double)s->slots[k].req.params.Nx * s->slots[k].req.params.Ny;
+    }
+  if (!any) return false;
+  if (s->lists_dirty) rebuild_lists(s);
+  int K = K_fixed;
+  if (K <= 0) {
+    const double step_s = active_cells / s->rate_est;
+    K = 1;
+    while (K < 64 && (K * 2) * step_s < 3e-3) K *= 2;
+  }
+  cudaGraphExec_t g = get_graph(s, K, s->mask);
+  const double t_start = s->now();
+  cudaEventRecord(s->ev0, s->stream);
+  if (g)
+    cudaGraphLaunch(g, s->stream);
+  else
+    for (int k = 0; k < K; ++k) launch_step(s, s->mask);
+  cudaEventRecord(s->ev1, s->stream);
+  int hi = 0;
+  for (int k = 0; k < s->max_sims; ++k)
+    if (s->slots[k].used) hi = k + 1;
+  cudaMemcpyAsync(s->h_down, s->d_sims, sizeof(SimDev) * hi, cudaMemcpyDeviceToHost, s->stream);
+  cudaStreamSynchronize(s->stream);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  s->replays++;
+  s->busy_s += s->now() - t_start;
+  double cells = 0;
+  std::vector<int> done;
+  for (int k = 0; k < hi; ++k) {
+    Slot &sl = s->slots[k];
+    if (!sl.used) continue;
+    const SimDev &d = s->h_down[k];
+    const int new_steps = d.step - sl.steps_seen;
+    cells += (double)d.N * d.N * new_steps;
+    sl.steps_seen = d.step;
+    if (d.status == SIM_DONE || d.status == SIM_FAILED) done.push_back(k);
+  }
+  s->cell_updates += cells;
+  if (ms > 0.05 && cells > 0) s->rate_est = 0.5 * s->rate_est + 0.5 * (cells / (ms * 1e-3));
+  for (int k : done) retire(s, k, s->h_down[k]);
+  return true;
+}
+
+void worker_main(fv2d_server *s) {
+  cudaSetDevice(s->device);
+  while (!s->stop.load()) {
+    std::vector<Pending> take;
+    {
+      std::unique_lock<std::mutex> lock(s->mu);
+      bool active = false;
+      for (auto &sl : s->slots)
+        if (sl.used) {
+          active = true;
+          break;
+        }
+      if (!active && s->queue.empty())
+        s->cv.wait_for(lock, std::chrono::milliseconds(20));
+      take.assign(s->queue.begin(), s->queue.end());
+      s->queue.clear();
+    }
+    // admission: first in, first out; a request that does not fit waits and
+    // smaller ones behind it may pass
+    std::vector<Pending> keep;
+    std::vector<int> fresh;
+    for (auto &pd : take) {
+      const int slot = admit(s, pd);
+      if (slot >= 0)
+        fresh.push_back(slot);
+      else
+        keep.push_back(pd);
+    }
+    if (!keep.empty()) {
+      std::lock_guard<std::mutex> lock(s->mu);
+      for (auto it = keep.rbegin(); it != keep.rend(); ++it) s->queue.push_front(*it);
+    }
+    read_initial_cons(s, fresh);
+    run_once(s, s->cfg.steps_per_replay);
+  }
+}
+
+// Autotuner: for each bucket, time every tile configuration on a synthetic
+// batch (Sedov states at the bucket's representative size) and keep the
+// fastest.
+void autotune(fv2d_server *s) {
+  const int rep[kBuckets] = {96, 192, 384, 768};
+  const int ncfg = batch_num_cfgs();
+  for (int b = 0; b < kBuckets; ++b) {
+    const int N = rep[b];
+    const int nsims = std::max(2, (int)(24e6 / ((double)N * N)));
+    double best = -1;
+    int best_cfg = s->bucket_cfg[b];
+    for (int c = 0; c < ncfg; ++c) {
+      if (!s->cfg_grid[c]) continue;
+      s->bucket_cfg[b] = c;
+      std::vector<int> used;
+      for (int k = 0; k < nsims; ++k) {
+        Pending pd;
+        pd.id = -1 - k;
+        std::memset(&pd.req, 0, sizeof(pd.req));
+        pd.req.struct_size = sizeof(fv2d_request);
+        pd.req.problem = FV2D_PB_SEDOV;
+        params_default(&pd.req.params);
+        pd.req.params.Nx = pd.req.params.Ny = N;
+        pd.req.params.gamma0 = 1.4;
+        pd.req.params.reconstruction = FV2D_PLM;
+        pd.req.params.riemann_solver = FV2D_HLLC;
+        pd.req.max_steps = 1 << 30;
+        pd.req.tend = 0;
+        pd.submit_s = 0;
+        if (admit(s, pd) < 0) break;
+      }
+      rebuild_lists(s);
+      for (int k = 0; k < 2; ++k) launch_step(s, s->mask);
+      cudaEventRecord(s->ev0, s->stream);
+      const int steps = 6;
+      for (int k = 0; k < steps; ++k) launch_step(s, s->mask);
+      cudaEventRecord(s->ev1, s->stream);
+      cudaStreamSynchronize(s->stream);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+      double cells = 0;
+      for (int k = 0; k < s->max_sims; ++k)
+        if (s->slots[k].used) cells += (double)N * N;
+      const double rate = cells * steps / (ms * 1e-3);
+      if (cudaGetLastError() == cudaSuccess && rate > best) {
+        best = rate;
+        best_cfg = c;
+      }
+      for (int k = 0; k < s->max_sims; ++k)
+        if (s->slots[k].used) {
+          s->arena.release(s->slots[k].mem, s->slots[k].bytes);
+          s->slots[k].used = false;
+          s->h_up[k].status = SIM_FREE;
+          s->free_slots.push_back(k);
+        }
+      cudaMemcpyAsync(s->d_sims, s->h_up, sizeof(SimDev) * s->max_sims, cudaMemcpyHostToDevice, s->stream);
+      s->n_admitted = 0;
+      s->lists_dirty = true;
+    }
+    s->bucket_cfg[b] = best_cfg;
+  }
+  cudaStreamSynchronize(s->stream);
+  s->free_slots.clear();
+  for (int k = s->max_sims - 1; k >= 0; --k) s->free_slots.push_back(k);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fv2d_server_config_name(int index) {
+  if (index < 0 || index >= batch_num_cfgs()) return nullptr;
+  const char *name;
+  batch_cfg_info(index, nullptr, nullptr, nullptr, nullptr, nullptr, &name);
+  return name;
+}
+
+int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
+  if (!cfg || !out || cfg->struct_size != sizeof(fv2d_server_config)) return FV2D_ERR_INVALID;
+  if (cfg->max_sims <= 0 || cfg->max_sims > 16384 || !(cfg->budget_bytes > 0)) return FV2D_ERR_INVALID;
+  *out = nullptr;
+  fv2d_server *s = new (std::nothrow) fv2d_server();
+  if (!s) return FV2D_ERR_NOMEM;
+  s->cfg = *cfg;
+  s->t0 = std::chrono::steady_clock::now();
+  s->device = cfg->device;
+  if (cudaSetDevice(s->device) != cudaSuccess) {
+    delete s;
+    return FV2D_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device);
+  s->max_sims = cfg->max_sims;
+  s->arena.budget = cfg->budget_bytes;
+  bool ok = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaMalloc(&s->d_sims, sizeof(SimDev) * s->max_sims) == cudaSuccess &&
+            cudaMallocHost(&s->h_up, sizeof(SimDev) * s->max_sims) == cudaSuccess &&
+            cudaMallocHost(&s->h_down, sizeof(SimDev) * s->max_sims) == cudaSuccess &&
+            cudaMalloc(&s->d_tmaps, sizeof(CUtensorMap) * 2 * s->max_sims) == cudaSuccess &&
+            cudaMallocHost(&s->h_tmaps, sizeof(CUtensorMap) * 2 * s->max_sims) == cudaSuccess &&
+            cudaMalloc(&s->d_nwork, sizeof(int) * kBuckets) == cudaSuccess &&
+            cudaMallocHost(&s->h_nwork, sizeof(int) * kBuckets) == cudaSuccess &&
+            cudaMalloc(&s->d_cons, sizeof(double) * kConsBlocks * 8 * s->max_sims) == cudaSuccess &&
+            cudaMallocHost(&s->h_cons, sizeof(double) * kConsBlocks * 8 * s->max_sims) == cudaSuccess &&
+            cudaEventCreate(&s->ev0) == cudaSuccess && cudaEventCreate(&s->ev1) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    fv2d_server_destroy(s);
+    return FV2D_ERR_NOMEM;
+  }
+  std::memset(s->h_up, 0, sizeof(SimDev) * s->max_sims);
+  cudaMemcpy(s->d_sims, s->h_up, sizeof(SimDev) * s->max_sims, cudaMemcpyHostToDevice);
+  std::memset(s->h_nwork, 0, sizeof(int) * kBuckets);
+  cudaMemcpy(s->d_nwork, s->h_nwork, sizeof(int) * kBuckets, cudaMemcpyHostToDevice);
+  s->slots.resize(s->max_sims);
+  for (int k = s->max_sims - 1; k >= 0; --k) s->free_slots.push_back(k);
+  for (int c = 0; c < batch_num_cfgs(); ++c) {
+    int per_sm = 0;
+    if (batch_setup(c, &per_sm) == cudaSuccess && per_sm > 0) s->cfg_grid[c] = per_sm * s->num_sms;
+  }
+  if (cfg->autotune) autotune(s);
+  s->worker = std::thread(worker_main, s);
+  *out = s;
+  return FV2D_OK;
+}
+
+int fv2d_server_destroy(fv2d_server *s) {
+  if (!s) return FV2D_ERR_INVALID;
+  s->stop.store(true);
+  s->cv.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (auto &g : s->graphs) cudaGraphExecDestroy(g.second);
+  s->arena.free_all();
+  for (int b = 0; b < kBuckets; ++b) {
+    if (s->d_work[b]) cudaFree(s->d_work[b]);
+    if (s->h_work[b]) cudaFreeHost(s->h_work[b]);
+  }
+  if (s->d_sims) cudaFree(s->d_sims);
+  if (s->h_up) cudaFreeHost(s->h_up);
+  if (s->h_down) cudaFreeHost(s->h_down);
+  if (s->d_tmaps) cudaFree(s->d_tmaps);
+  if (s->h_tmaps) cudaFreeHost(s->h_tmaps);
+  if (s->d_nwork) cudaFree(s->d_nwork);
+  if (s->h_nwork) cudaFreeHost(s->h_nwork);
+  if (s->d_cons) cudaFree(s->d_cons);
+  if (s->h_cons) cudaFreeHost(s->h_cons);
+  if (s->h_stage) cudaFreeHost(s->h_stage);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return FV2D_OK;
+}
+
+int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id) {
+  if (!s || !req || !id) return FV2D_ERR_INVALID;
+  if (check_request(*req)) return FV2D_ERR_UNSUPPORTED;
+  int pitch;
+  long long plane;
+  if ((double)state_bytes(req->params.Nx, &pitch, &plane) > s->cfg.budget_bytes) return FV2D_ERR_SIZE;
+  std::lock_guard<std::mutex> lock(s->mu);
+  Pending pd;
+  pd.id = s->next_id++;
+  pd.req = *req;
+  pd.submit_s = s->now();
+  s->queue.push_back(pd);
+  s->n_submitted++;
+  *id = pd.id;
+  s->cv.notify_all();
+  return FV2D_OK;
+}
+
+int fv2d_server_poll(fv2d_server *s, fv2d_result *out, int max, int *n) {
+  if (!s || !n || (max > 0 && !out)) return FV2D_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  const int k = std::min<int>(max, (int)s->done_unpolled.size());
+  for (int i = 0; i < k; ++i) out[i] = s->done_unpolled[i];
+  s->done_unpolled.erase(s->done_unpolled.begin(), s->done_unpolled.begin() + k);
+  *n = k;
+  return FV2D_OK;
+}
+
+int fv2d_server_drain(fv2d_server *s, double timeout_s) {
+  if (!s) return FV2D_ERR_INVALID;
+  const double end = s->now() + timeout_s;
+  std::unique_lock<std::mutex> lock(s->mu);
+  for (;;) {
+    const bool idle = s->queue.empty() && (s->n_completed + s->n_failed) == s->n_submitted;
+    if (idle) return FV2D_OK;
+    if (s->now() > end) return FV2D_ERR_STATE;
+    s->cv.wait_for(lock, std::chrono::milliseconds(5));
+  }
+}
+
+int fv2d_server_get_prim(fv2d_server *s, int64_t id, double *q) {
+  if (!s || !q) return FV2D_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->finished.find(id);
+  if (it == s->finished.end()) return FV2D_ERR_STATE;
+  const Finished &f = it->second;
+  const int N = f.res.N;
+  const size_t n = (size_t)N * N;
+  const double gm1 = f.gamma - 1.0;
+  for (size_t c = 0; c < n; ++c) {
+    const double r = f.U[c], mu = f.U[n + c], mv = f.U[2 * n + c], E = f.U[3 * n + c];
+    const double u = mu / r, v = mv / r;
+    q[4 * c] = r;
+    q[4 * c + 1] = u;
+    q[4 * c + 2] = v;
+    q[4 * c + 3] = (E - 0.5 * r * (u * u + v * v)) * gm1;
+  }
+  return FV2D_OK;
+}
+
+int fv2d_server_release(fv2d_server *s, int64_t id) {
+  if (!s) return FV2D_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  return s->finished.erase(id) ? FV2D_OK : FV2D_ERR_STATE;
+}
+
+int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out) {
+  if (!s || !out) return FV2D_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->submitted = s->n_submitted;
+  out->admitted = s->n_admitted;
+  out->completed = s->n_completed;
+  out->failed = s->n_failed;
+  int active = 0;
+  for (auto &sl : s->slots) active += sl.used;
+  out->active = active;
+  out->queued = (int)s->queue.size();
+  out->cell_updates = s->cell_updates;
+  out->busy_s = s->busy_s;
+  out->bytes_in_use = (double)s->arena.in_use;
+  out->bytes_reserved = (double)s->arena.reserved;
+  for (int b = 0; b < kBuckets; ++b) out->bucket_cfg[b] = s->bucket_cfg[b];
+  out->replays = s->replays;
+  return FV2D_OK;
+}
+
+}  // extern "C"

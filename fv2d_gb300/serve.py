@@ -1,0 +1,172 @@
+"""ctypes binding of the batched FP32 service (include/fv2d_serve.h) and the
+seeded request stream used by the benchmark and the tests."""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import lib as _lib_loader
+from ._abi import Params, PROBLEMS, as_float32
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("device", C.c_int32), ("budget_bytes", C.c_double),
+                ("max_sims", C.c_int32), ("autotune", C.c_int32), ("steps_per_replay", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("problem", C.c_int32), ("params", Params),
+                ("max_steps", C.c_int32), ("lowmach", C.c_int32), ("tend", C.c_double)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("steps", C.c_int32), ("t", C.c_double),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
+                ("cons0", C.c_double * 4), ("cons1", C.c_double * 4), ("negatives", C.c_uint64),
+                ("N", C.c_int32), ("bucket", C.c_int32)]
+
+    def as_dict(self):
+        d = {n: getattr(self, n) for n, _ in self._fields_}
+        d["cons0"] = list(self.cons0)
+        d["cons1"] = list(self.cons1)
+        return d
+
+
+class Stats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
+                ("failed", C.c_int64), ("active", C.c_int32), ("queued", C.c_int32),
+                ("cell_updates", C.c_double), ("busy_s", C.c_double), ("bytes_in_use", C.c_double),
+                ("bytes_reserved", C.c_double), ("bucket_cfg", C.c_int32 * 4), ("replays", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+def _bind(L):
+    if getattr(L, "_serve_bound", False):
+        return L
+    vp = C.c_void_p
+    L.fv2d_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
+    L.fv2d_server_destroy.argtypes = [vp]
+    L.fv2d_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_int64)]
+    L.fv2d_server_poll.argtypes = [vp, C.POINTER(Result), C.c_int, C.POINTER(C.c_int)]
+    L.fv2d_server_drain.argtypes = [vp, C.c_double]
+    L.fv2d_server_get_prim.argtypes = [vp, C.c_int64, C.POINTER(C.c_double)]
+    L.fv2d_server_release.argtypes = [vp, C.c_int64]
+    L.fv2d_server_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.fv2d_server_config_name.argtypes = [C.c_int]
+    L.fv2d_server_config_name.restype = C.c_char_p
+    L._serve_bound = True
+    return L
+
+
+def config_name(index):
+    v = _bind(_lib_loader()).fv2d_server_config_name(index)
+    return v.decode() if v else None
+
+
+class Server:
+    """A running batched service on one GPU."""
+
+    def __init__(self, budget_bytes=150e9, device=0, max_sims=4096, autotune=True, steps_per_replay=0):
+        self.L = _bind(_lib_loader())
+        cfg = ServerConfig(C.sizeof(ServerConfig), device, float(budget_bytes), max_sims, 1 if autotune else 0,
+                           steps_per_replay, 0)
+        self.h = C.c_void_p()
+        rc = self.L.fv2d_server_create(C.byref(cfg), C.byref(self.h))
+        if rc != 0:
+            raise RuntimeError(f"fv2d_server_create failed ({rc})")
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fv2d_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, problem, params, max_steps, tend=0.0, lowmach=False):
+        pb = PROBLEMS[problem] if isinstance(problem, str) else int(problem)
+        r = Request(C.sizeof(Request), pb, params, int(max_steps), 1 if lowmach else 0, float(tend))
+        i = C.c_int64()
+        rc = self.L.fv2d_server_submit(self.h, C.byref(r), C.byref(i))
+        if rc != 0:
+            raise ValueError(f"request rejected ({rc})")
+        self._n[i.value] = params.Nx
+        return i.value
+
+    def poll(self, max_results=1024):
+        out = (Result * max_results)()
+        n = C.c_int()
+        self.L.fv2d_server_poll(self.h, out, max_results, C.byref(n))
+        return [out[k] for k in range(n.value)]
+
+    def drain(self, timeout_s=600.0):
+        return self.L.fv2d_server_drain(self.h, float(timeout_s))
+
+    def get_prim(self, rid):
+        N = self._n[rid]
+        q = np.empty((N, N, 4))
+        rc = self.L.fv2d_server_get_prim(self.h, rid, q.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != 0:
+            raise KeyError(rid)
+        return q
+
+    def release(self, rid):
+        self.L.fv2d_server_release(self.h, rid)
+
+    def stats(self):
+        s = Stats()
+        self.L.fv2d_server_get_stats(self.h, C.byref(s))
+        return s
+
+
+def stream_requests(n=512, rate=200.0, seed=12345, nmin=64, nmax=1024, steps=(200, 2000)):
+    """The benchmark's request stream: a seeded Poisson arrival process;
+    grid N log-uniform in [nmin, nmax] rounded to a multiple of 32; initial
+    condition uniform over Sod (density ratio 2..20), Sedov (E0 0.5..2),
+    Kelvin-Helmholtz (shear speed 0.2..1) and Gresho (rho = 1, Mach
+    0.01..0.1); gamma uniform in [1.3, 1.67]; 200..2000 steps.  Returns a
+    list of dicts with arrival time, problem, params and step count."""
+    from . import default_params, PLM, HLLC, BC_ABSORBING, BC_REFLECTING, BC_PERIODIC
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(n):
+        t += rng.exponential(1.0 / rate)
+        N = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax))) / 32.0)) * 32
+        N = min(max(N, nmin), nmax)
+        kind = ["sod", "sedov", "kh", "gresho"][int(rng.integers(0, 4))]
+        gamma = float(rng.uniform(1.3, 1.67))
+        nsteps = int(rng.integers(steps[0], steps[1] + 1))
+        f = as_float32
+        p = default_params(Nx=N, Ny=N, gamma0=f(gamma), CFL=f(0.8), reconstruction=PLM, riemann_solver=HLLC)
+        lowmach = False
+        if kind == "sod":
+            ratio = float(rng.uniform(2.0, 20.0))
+            p.update(boundary_x=BC_ABSORBING, boundary_y=BC_PERIODIC, sod_rho_left=1.0, sod_p_left=1.0,
+                     sod_rho_right=1.0 / ratio, sod_p_right=0.1)
+            problem = "sod_x"
+        elif kind == "sedov":
+            p.update(boundary_x=BC_REFLECTING, boundary_y=BC_REFLECTING, sedov_E0=float(rng.uniform(0.5, 2.0)))
+            problem = "sedov"
+        elif kind == "kh":
+            p.update(boundary_x=BC_PERIODIC, boundary_y=BC_PERIODIC, khs_u=float(rng.uniform(0.2, 1.0)),
+                     seed=int(rng.integers(1, 1 << 30)))
+            problem = "kh_step"
+        else:
+            p.update(boundary_x=BC_PERIODIC, boundary_y=BC_PERIODIC, gresho_density=1.0,
+                     gresho_Mach=f(float(rng.uniform(0.01, 0.1))))
+            problem = "gresho_vortex"
+            lowmach = True
+        out.append(dict(arrival=t, problem=problem, params=p, steps=nsteps, N=N, kind=kind, lowmach=lowmach))
+    return out

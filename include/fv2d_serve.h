@@ -1,0 +1,107 @@
+/*
+ * fv2d_serve.h -- batched FP32 service of libfv2d_gpu.so: many independent
+ * fv2d simulations of different sizes admitted as they arrive and advanced
+ * together on one GB300.
+ *
+ * No counterpart in the reference (which runs one simulation per process,
+ * main.cpp:13-101); each simulation follows the reference's step
+ * (ComputeDt.h:18-65, Update.h:93-191, SimInfo.h:576-646) in binary32
+ * storage and flux arithmetic, with the simulation clock, dt, the
+ * conservation sums and (for low-Mach requests) the internal-energy
+ * recovery E - rho|u|^2/2 in binary64.
+ *
+ * Serving model:
+ *   - fv2d_server_submit queues a request; a worker thread admits queued
+ *     requests (first in, first out, smaller ones may pass a request that
+ *     does not fit) while the HBM budget and the simulation table allow;
+ *   - every admitted state stays resident in HBM until it completes;
+ *   - all admitted simulations advance together: per grid-size bucket one
+ *     persistent kernel launch per step walks a (simulation, tile) work list,
+ *     each simulation reduces its own dt; a CUDA graph replays several steps
+ *     between admissions and retirements;
+ *   - tile shape, threads per tile and halo staging are chosen per bucket by
+ *     an autotuner at start-up (or fixed defaults).
+ * A simulation's result does not depend on what else was in the batch.
+ */
+#ifndef FV2D_SERVE_H
+#define FV2D_SERVE_H
+
+#include "fv2d_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fv2d_server fv2d_server;
+
+typedef struct fv2d_server_config {
+  uint32_t struct_size;
+  int32_t device;           /* CUDA device */
+  double budget_bytes;      /* HBM budget for simulation states (admission control) */
+  int32_t max_sims;         /* simulation table capacity (<= 16384) */
+  int32_t autotune;         /* 1: time the tile configurations per bucket at start-up */
+  int32_t steps_per_replay; /* 0: adaptive (about 3 ms of work per graph replay) */
+  int32_t pad;
+} fv2d_server_config;
+
+typedef struct fv2d_request {
+  uint32_t struct_size;
+  int32_t problem;   /* FV2D_PB_* initial condition */
+  fv2d_params params;/* Nx == Ny == N (multiple of 32, 64..4096); PCM or PLM; HLL or HLLC; Euler;
+                        constant gravity, constant conductivity and viscosity allowed */
+  int32_t max_steps; /* stop after this many steps */
+  int32_t lowmach;   /* 1: recover the pressure from E - rho|u|^2/2 in binary64 */
+  double tend;       /* also stop once t + epsilon >= tend (<= 0: no time limit) */
+} fv2d_request;
+
+typedef struct fv2d_result {
+  int64_t id;
+  int32_t status;    /* FV2D_OK, or FV2D_ERR_NUMERIC when the dt guard stopped it */
+  int32_t steps;     /* steps taken */
+  double t;          /* simulation time reached (binary64 clock) */
+  double submit_s, admit_s, done_s;  /* server clock, seconds since fv2d_server_create */
+  double cons0[4];   /* sum over cells of (rho, rho u, rho v, E) * dx * dy at admission, */
+  double cons1[4];   /* and at completion: compensated binary64 sums of the binary32 state */
+  uint64_t negatives;/* cells reset by the negative density/pressure guard */
+  int32_t N;
+  int32_t bucket;
+} fv2d_result;
+
+typedef struct fv2d_server_stats {
+  int64_t submitted, admitted, completed, failed;
+  int32_t active, queued;
+  double cell_updates;   /* total cell-updates performed */
+  double busy_s;         /* wall time with at least one active simulation */
+  double bytes_in_use;   /* HBM held by resident states */
+  double bytes_reserved; /* HBM reserved by the state arena */
+  int32_t bucket_cfg[4]; /* configuration index chosen per bucket (see fv2d_server_config_name) */
+  int32_t replays;       /* graph replays launched */
+  int32_t pad;
+} fv2d_server_stats;
+
+int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out);
+int fv2d_server_destroy(fv2d_server *s);
+
+/* Queue a request; returns its id.  Thread-safe. */
+int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id);
+
+/* Results completed since the last poll (at most max); *n receives the count. */
+int fv2d_server_poll(fv2d_server *s, fv2d_result *out, int max, int *n);
+
+/* Block until nothing is queued or running (or timeout_s elapses). */
+int fv2d_server_drain(fv2d_server *s, double timeout_s);
+
+/* Final primitive state of a completed request (N x N x {rho,u,v,p}, binary64
+ * values of the binary32 state), until fv2d_server_release. */
+int fv2d_server_get_prim(fv2d_server *s, int64_t id, double *q_host);
+int fv2d_server_release(fv2d_server *s, int64_t id);
+
+int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out);
+
+/* Name of tile configuration `index` ("32x16/256/tma", ...); NULL if none. */
+const char *fv2d_server_config_name(int index);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FV2D_SERVE_H */

@@ -1,0 +1,135 @@
+"""The batched FP32 service (include/fv2d_serve.h), through the C-ABI.
+
+* A request's result is identical (bit for bit) alone and in a mixed batch.
+* Accuracy against the binary64 plain path (bit-identical to the reference):
+  L1 relative error of rho and p after the same number of steps, and the
+  conservation drift of the binary64 sums.
+* Admission control: with a budget that holds two states at a time every
+  request still completes, never more than fits are resident.
+"""
+import numpy as np
+import pytest
+
+from fv2d_testlib import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def params(N, **kw):
+    import fv2d_gb300 as fv
+    f = fv.as_float32
+    base = dict(Nx=N, Ny=N, gamma0=f(1.4), CFL=f(0.8), reconstruction=fv.PLM, riemann_solver=fv.HLLC,
+                boundary_x=fv.BC_REFLECTING, boundary_y=fv.BC_REFLECTING)
+    base.update(kw)
+    return fv.default_params(**base)
+
+
+def mixed_requests():
+    import fv2d_gb300 as fv
+    return [
+        ("sedov", params(128), 60, False),
+        ("sod_x", params(256, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC), 80, False),
+        ("kh_step", params(96, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC, seed=7), 50, False),
+        ("gresho_vortex", params(64, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC,
+                                 gresho_Mach=fv.as_float32(0.05)), 100, True),
+        ("rt_hydrostatic", params(160, riemann_solver=fv.HLL, boundary_x=fv.BC_PERIODIC, xmax=0.5, ymax=1.5,
+                                  gravity_mode=fv.GRAV_CONSTANT, gy=-0.1, thermal_conductivity_active=1,
+                                  kappa=1e-4, viscosity_active=1, mu=1e-4), 40, False),
+    ]
+
+
+def test_same_result_alone_and_in_the_mix(gpu_lib):
+    from fv2d_gb300.serve import Server
+    reqs = mixed_requests()
+    alone = []
+    with Server(budget_bytes=4e9, autotune=False) as s:
+        for pb, p, n, lm in reqs:
+            rid = s.submit(pb, p, n, lowmach=lm)
+            assert s.drain(120) == 0
+            res = {r.id: r for r in s.poll()}
+            assert res[rid].status == 0 and res[rid].steps == n
+            alone.append((s.get_prim(rid), res[rid].t))
+    with Server(budget_bytes=4e9, autotune=False) as s:
+        fillers = [s.submit("sedov", params(N), 30 + N // 16) for N in (64, 320, 512, 192, 96)]
+        ids = [s.submit(pb, p, n, lowmach=lm) for pb, p, n, lm in reqs]
+        fillers += [s.submit("kh_step", params(N, boundary_x=2, boundary_y=2), 45) for N in (128, 224)]
+        assert s.drain(120) == 0
+        res = {r.id: r for r in s.poll()}
+        assert all(res[i].status == 0 for i in ids + fillers)
+        for k, rid in enumerate(ids):
+            q, t = alone[k]
+            assert res[rid].t == t, reqs[k][0]
+            assert bits_equal(s.get_prim(rid), q), reqs[k][0]
+
+
+def l1_rel(a, b):
+    return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
+
+
+def test_accuracy_against_fp64_path(gpu_lib):
+    """Each request against the binary64 plain path from the same initial
+    condition after the same number of steps."""
+    import fv2d_gb300 as fv
+    from fv2d_gb300.serve import Server
+    cases = [
+        ("sod_x", params(256, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC), 200, False),
+        ("sedov", params(256), 200, False),
+        ("kh_step", params(256, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC), 200, False),
+        ("gresho_vortex", params(128, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC,
+                                 gresho_Mach=fv.as_float32(0.1)), 200, True),
+    ]
+    report = {}
+    with Server(budget_bytes=4e9, autotune=False) as s:
+        ids = [s.submit(pb, p, n, lowmach=lm) for pb, p, n, lm in cases]
+        assert s.drain(120) == 0
+        res = {r.id: r for r in s.poll()}
+        for (pb, p, n, lm), rid in zip(cases, ids):
+            sim = fv.Simulation(p)
+            sim.init_problem(pb)
+            sim.advance(n, 1e30)
+            q64 = sim.get_prim()
+            q32 = s.get_prim(rid)
+            r = res[rid]
+            drift = abs(r.cons1[0] - r.cons0[0]) / abs(r.cons0[0])
+            report[pb] = (l1_rel(q32[..., 0], q64[..., 0]), l1_rel(q32[..., 3], q64[..., 3]), drift)
+            sim.close()
+    print(report)
+    for pb, (erho, ep, drift) in report.items():
+        assert erho < 1e-4 and ep < 1e-4, (pb, erho, ep)
+    # closed domains conserve mass to binary32 rounding of the state
+    for pb in ("sedov", "kh_step", "gresho_vortex"):
+        assert report[pb][2] < 1e-6, (pb, report[pb])
+
+
+def test_admission_respects_budget(gpu_lib):
+    from fv2d_gb300.serve import Server
+    # one 256^2 state pair is 8 * 260 * 288 * 4 B = 2.4 MB; budget for two
+    budget = 2.0 * 8 * 260 * 288 * 4 + 1024
+    with Server(budget_bytes=budget, autotune=False) as s:
+        ids = [s.submit("sedov", params(256), 40) for _ in range(6)]
+        peak = 0
+        import time
+        t0 = time.time()
+        while time.time() - t0 < 60:
+            st = s.stats()
+            peak = max(peak, st.active)
+            if st.completed == 6:
+                break
+            time.sleep(0.002)
+        assert s.drain(60) == 0
+        res = s.poll()
+        assert sorted(r.id for r in res) == sorted(ids)
+        assert peak <= 2
+        assert s.stats().bytes_reserved <= budget
+
+
+def test_rejects_unsupported_requests(gpu_lib):
+    import fv2d_gb300 as fv
+    from fv2d_gb300.serve import Server
+    with Server(budget_bytes=1e9, autotune=False) as s:
+        for bad in (dict(time_stepping=fv.TS_RK2), dict(riemann_solver=fv.FSLP), dict(Ny=96),
+                    dict(reconstruction=fv.MUSCL_HANCOCK)):
+            with pytest.raises(ValueError):
+                s.submit("sedov", params(128, **bad), 10)
+        with pytest.raises(ValueError):
+            s.submit("sedov", params(100), 10)  # not a multiple of 32
