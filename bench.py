@@ -274,6 +274,9 @@ def main():
     ap.add_argument("--no-4096", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-requests", type=int, default=512)
+    ap.add_argument("--served-only", action="store_true", help="only the batched FP32 service on the stream")
+    ap.add_argument("--served-profile", action="store_true",
+                    help="fixed batch for kernel profiling: 12 Sedov 768^2 requests x 60 steps")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -287,6 +290,22 @@ def main():
     if not os.path.exists(fv.LIB_PATH):
         from fv2d_gb300 import build as b
         b.build()
+    if args.served_profile:
+        from fv2d_gb300.serve import Server
+        with Server(budget_bytes=20e9, device=local, autotune=False) as srv:
+            p = workload_params(fv, 768)
+            for _ in range(12):
+                srv.submit("sedov", p, 60)
+            srv.drain(300)
+            st = srv.stats()
+            print(json.dumps({"served_profile": True, "completed": st.completed, "cell_updates": st.cell_updates,
+                              "busy_s": st.busy_s}), flush=True)
+        return
+    if args.served_only:
+        t0 = time.perf_counter()
+        served = run_served(fv, n_requests=args.served_requests, device=local)
+        print(json.dumps({"metric": METRIC, "served": served, "wall_s": time.perf_counter() - t0}), flush=True)
+        return
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
