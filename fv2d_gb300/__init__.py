@@ -221,7 +221,9 @@ class Simulation:
         self._check(self._lib.fv2d_set_time(self.h, float(t), int(iteration)))
 
     def step_log(self, max_records=4096):
-        rec = np.empty((max_records, 3))
+        """Per-iteration records of the last device-driven run: columns t, dt,
+        inv_dt_hyp, negative density, negative pressure, NaN counts."""
+        rec = np.empty((max_records, 6))
         n = C.c_int()
         self._check(self._lib.fv2d_get_step_log(self.h, _ptr(rec), max_records, C.byref(n)))
         return rec[: n.value].copy()

@@ -45,7 +45,11 @@ UNITS = [
     ("batch_kernels.cu", ["-use_fast_math"]),
     ("serve.cu", []),
     ("problems.cpp", []),
+    ("../host/ini.cpp", []),
+    ("../host/h5.cpp", []),
+    ("../host/io_api.cpp", []),
 ]
+DRIVER = os.path.join(PKG, "bin", "fv2d_gpu")
 
 
 def _headers():
@@ -73,12 +77,13 @@ def build(verbose=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     nvcc = _nvcc()
-    hdr_mtime = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(__file__)])
+    hdr_mtime = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(__file__)] +
+                    [os.path.getmtime(h) for h in glob.glob(os.path.join(PKG, "host", "*.hpp"))])
     # objects built on another host architecture are never reused
     stamp = os.path.join(BUILD, "host-arch")
     arch = platform.machine()
     if not os.path.exists(stamp) or open(stamp).read().strip() != arch:
-        for f in glob.glob(os.path.join(BUILD, "*.o")) + [LIB]:
+        for f in glob.glob(os.path.join(BUILD, "*.o")) + [LIB, DRIVER]:
             if os.path.exists(f):
                 os.unlink(f)
         with open(stamp, "w") as f:
@@ -86,7 +91,7 @@ def build(verbose=False, jobs=None):
     cmds, objs = [], []
     for src, extra in UNITS:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+        o = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(o)
         if not _stale(o, s, hdr_mtime):
             continue
@@ -94,7 +99,7 @@ def build(verbose=False, jobs=None):
             cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
                    *extra, "-c", s, "-o", o]
         else:
-            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", s, "-o", o]
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-c", s, "-o", o]
         cmds.append(cmd)
     if cmds:
         with ThreadPoolExecutor(max_workers=jobs or min(8, len(cmds))) as ex:
@@ -103,6 +108,12 @@ def build(verbose=False, jobs=None):
                     print(out)
     if cmds or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         _compile([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fPIC"])
+    # the fv2d_gpu driver executable (main.cpp's role), linked to the library
+    drv_src = os.path.join(PKG, "host", "driver.cpp")
+    if not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < max(os.path.getmtime(LIB), os.path.getmtime(drv_src)):
+        os.makedirs(os.path.dirname(DRIVER), exist_ok=True)
+        _compile(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", drv_src, "-o", DRIVER,
+                  "-L" + LIBDIR, "-lfv2d_gpu", "-Wl,-rpath,$ORIGIN/../lib"])
     return LIB
 
 

@@ -458,7 +458,7 @@ int fv2d_create(const fv2d_params *p, int device, fv2d_ctx **out) {
     return bail(FV2D_ERR_NOMEM);
   }
   ctx->log_cap = 4096;
-  if (cudaMalloc(&ctx->log, sizeof(double) * 3 * ctx->log_cap) != cudaSuccess) {
+  if (cudaMalloc(&ctx->log, sizeof(double) * 6 * ctx->log_cap) != cudaSuccess) {
     cudaGetLastError();
     ctx->err = "device allocation failed";
     return bail(FV2D_ERR_NOMEM);
@@ -660,7 +660,7 @@ int fv2d_get_step_log(fv2d_ctx *ctx, double *records, int max_records, int *coun
   if (int rc = sync_state(ctx)) return rc;
   int n = std::min(std::min(ctx->st_host->steps_in_call, ctx->log_cap), max_records);
   if (n > 0) {
-    CK(cudaMemcpyAsync(records, ctx->log, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(records, ctx->log, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
   if (count) *count = n;

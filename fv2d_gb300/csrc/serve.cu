@@ -130,24 +130,24 @@ __global__ void __launch_bounds__(256) cons_kernel(const SimDev *sims, int slot,
     const long long g = (long long)(j + 2) * S.pitch + (i + 2);
     for (int f = 0; f < 4; ++f) neumaier_add(s[f], c[f], (double)U[f * S.plane + g]);
   }
+  // pairwise tree over the block, carrying the compensation terms
   __shared__ double sh[8][256];
   for (int f = 0; f < 4; ++f) {
     sh[2 * f][threadIdx.x] = s[f];
     sh[2 * f + 1][threadIdx.x] = c[f];
   }
   __syncthreads();
-  if (threadIdx.x < 8) {
-    const int f = threadIdx.x >> 1, comp = threadIdx.x & 1;
-    if (comp == 0) {
-      double ss = 0, cc = 0;
-      for (int t = 0; t < 256; ++t) {
-        neumaier_add(ss, cc, sh[2 * f][t]);
-        cc += sh[2 * f + 1][t];
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int f = 0; f < 4; ++f) {
+        double a = sh[2 * f][threadIdx.x], ca = sh[2 * f + 1][threadIdx.x];
+        neumaier_add(a, ca, sh[2 * f][threadIdx.x + w]);
+        sh[2 * f][threadIdx.x] = a;
+        sh[2 * f + 1][threadIdx.x] = ca + sh[2 * f + 1][threadIdx.x + w];
       }
-      out[(blockIdx.x * 4 + f) * 2] = ss;
-      out[(blockIdx.x * 4 + f) * 2 + 1] = cc;
-    }
+    __syncthreads();
   }
+  if (threadIdx.x < 8) out[blockIdx.x * 8 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
 // ---------------------------------------------------------------- arena
@@ -424,7 +424,8 @@ int admit(fv2d_server *s, const Pending &pd) {
   const int nb = (int)std::min<long long>(1024, ((long long)N * N + 255) / 256);
   first_dt_kernel<<<nb, 256, 0, s->stream>>>(s->d_sims, slot);
   first_dt_finish<<<1, 1, 0, s->stream>>>(s->d_sims, slot);
-  cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
+  if (pd.id > 0)  // the autotuner's synthetic states need no sums
+    cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
   s->n_admitted++;
   s->lists_dirty = true;
   return slot;
@@ -524,59 +525,81 @@ cudaGraphExec_t get_graph(fv2d_server *s, int K, int mask) {
   return ex;
 }
 
-void retire(fv2d_server *s, int slot, const SimDev &d) {
-  Slot &sl = s->slots[slot];
-  const int N = d.N;
-  Finished fin;
-  fv2d_result &r = fin.res;
-  std::memset(&r, 0, sizeof(r));
-  r.id = sl.id;
-  r.status = d.status == SIM_DONE ? FV2D_OK : FV2D_ERR_NUMERIC;
-  r.steps = d.step;
-  r.t = d.t;
-  r.submit_s = sl.submit_s;
-  r.admit_s = sl.admit_s;
-  r.negatives = d.negatives;
-  r.N = N;
-  r.bucket = sl.bucket;
-  for (int f = 0; f < 4; ++f) r.cons0[f] = sl.cons0[f];
-  // final conservation sums and state
-  cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
-  cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
-                  sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
-  const size_t need = sizeof(float) * 4 * (size_t)N * N;
-  if (s->h_stage_size < need) {
-    if (s->h_stage) cudaFreeHost(s->h_stage);
-    cudaMallocHost(&s->h_stage, need);
-    s->h_stage_size = need;
+// Retire the finished simulations of one replay: final conservation sums and
+// state copies are queued for all of them, then one synchronisation.
+void retire_all(fv2d_server *s, const std::vector<int> &done) {
+  if (done.empty()) return;
+  size_t need = 0;
+  std::vector<size_t> off(done.size());
+  for (size_t k = 0; k < done.size(); ++k) {
+    off[k] = need;
+    const int N = s->h_down[done[k]].N;
+    need += 4 * (size_t)N * N;
   }
-  for (int f = 0; f < 4; ++f)
-    cudaMemcpy2DAsync(s->h_stage + (size_t)f * N * N, sizeof(float) * N, d.U[d.cur] + f * d.plane + 2 * d.pitch + 2,
-                      sizeof(float) * d.pitch, sizeof(float) * N, N, cudaMemcpyDeviceToHost, s->stream);
+  if (s->h_stage_size < need * sizeof(float)) {
+    if (s->h_stage) cudaFreeHost(s->h_stage);
+    cudaMallocHost(&s->h_stage, need * sizeof(float));
+    s->h_stage_size = need * sizeof(float);
+  }
+  for (size_t k = 0; k < done.size(); ++k) {
+    const int slot = done[k];
+    const SimDev &d = s->h_down[slot];
+    const int N = d.N;
+    cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
+    cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
+                    sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
+    for (int f = 0; f < 4; ++f)
+      cudaMemcpy2DAsync(s->h_stage + off[k] + (size_t)f * N * N, sizeof(float) * N,
+                        d.U[d.cur] + f * d.plane + 2 * d.pitch + 2, sizeof(float) * d.pitch, sizeof(float) * N, N,
+                        cudaMemcpyDeviceToHost, s->stream);
+    // mark the device slot free so stale work-list entries are skipped
+    s->h_up[slot].status = SIM_FREE;
+    cudaMemcpyAsync(&s->d_sims[slot].status, &s->h_up[slot].status, sizeof(int), cudaMemcpyHostToDevice,
+                    s->stream);
+  }
   cudaStreamSynchronize(s->stream);
-  double c1[4];
-  sum_cons(s->h_cons + (size_t)slot * kConsBlocks * 8, c1);
-  const fv2d_params &p = sl.req.params;
-  const double area = ((p.xmax - p.xmin) / p.Nx) * ((p.ymax - p.ymin) / p.Ny);
-  for (int f = 0; f < 4; ++f) r.cons1[f] = c1[f] * area;
-  fin.U.assign(s->h_stage, s->h_stage + 4 * (size_t)N * N);
-  fin.gamma = p.gamma0;
-  r.done_s = s->now();
-  s->arena.release(sl.mem, sl.bytes);
-  sl.used = false;
-  sl.mem = nullptr;
-  s->free_slots.push_back(slot);
-  s->lists_dirty = true;
-  // mark the device slot free so stale list entries are skipped
-  s->h_up[slot].status = SIM_FREE;
-  cudaMemcpyAsync(&s->d_sims[slot].status, &s->h_up[slot].status, sizeof(int), cudaMemcpyHostToDevice, s->stream);
-  std::lock_guard<std::mutex> lock(s->mu);
-  if (r.status == FV2D_OK)
-    s->n_completed++;
-  else
-    s->n_failed++;
-  s->done_unpolled.push_back(r);
-  s->finished.emplace(r.id, std::move(fin));
+  const double t_done = s->now();
+  for (size_t k = 0; k < done.size(); ++k) {
+    const int slot = done[k];
+    const SimDev &d = s->h_down[slot];
+    Slot &sl = s->slots[slot];
+    const int N = d.N;
+    Finished fin;
+    fv2d_result &r = fin.res;
+    std::memset(&r, 0, sizeof(r));
+    r.id = sl.id;
+    r.status = d.status == SIM_DONE ? FV2D_OK : FV2D_ERR_NUMERIC;
+    r.steps = d.step;
+    r.t = d.t;
+    r.submit_s = sl.submit_s;
+    r.admit_s = sl.admit_s;
+    r.negatives = d.negatives;
+    r.N = N;
+    r.bucket = sl.bucket;
+    const fv2d_params &p = sl.req.params;
+    const double area = ((p.xmax - p.xmin) / p.Nx) * ((p.ymax - p.ymin) / p.Ny);
+    double c1[4];
+    sum_cons(s->h_cons + (size_t)slot * kConsBlocks * 8, c1);
+    for (int f = 0; f < 4; ++f) {
+      r.cons0[f] = sl.cons0[f];
+      r.cons1[f] = c1[f] * area;
+    }
+    fin.U.assign(s->h_stage + off[k], s->h_stage + off[k] + 4 * (size_t)N * N);
+    fin.gamma = p.gamma0;
+    r.done_s = t_done;
+    s->arena.release(sl.mem, sl.bytes);
+    sl.used = false;
+    sl.mem = nullptr;
+    s->free_slots.push_back(slot);
+    s->lists_dirty = true;
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (r.status == FV2D_OK)
+      s->n_completed++;
+    else
+      s->n_failed++;
+    s->done_unpolled.push_back(r);
+    s->finished.emplace(r.id, std::move(fin));
+  }
   s->cv.notify_all();
 }
 
@@ -628,7 +651,7 @@ bool run_once(fv2d_server *s, int K_fixed) {
   }
   s->cell_updates += cells;
   if (ms > 0.05 && cells > 0) s->rate_est = 0.5 * s->rate_est + 0.5 * (cells / (ms * 1e-3));
-  for (int k : done) retire(s, k, s->h_down[k]);
+  retire_all(s, done);
   return true;
 }
 
@@ -677,7 +700,7 @@ void autotune(fv2d_server *s) {
   const int ncfg = batch_num_cfgs();
   for (int b = 0; b < kBuckets; ++b) {
     const int N = rep[b];
-    const int nsims = std::max(2, (int)(24e6 / ((double)N * N)));
+    const int nsims = std::max(2, std::min(256, (int)(24e6 / ((double)N * N))));
     double best = -1;
     int best_cfg = s->bucket_cfg[b];
     for (int c = 0; c < ncfg; ++c) {

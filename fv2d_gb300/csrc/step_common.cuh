@@ -53,7 +53,7 @@ struct StepArgs {
   const float *grav_row;  // analytical gravity per interior row (float, Gravity.h:16)
   const double *kap_row;  // per interior row: kappaL, kappaR, kappaU, kappaD
   DevState *st;
-  double *log;        // per-iteration records {t, dt, inv_hyp} (may be null)
+  double *log;        // per-iteration records {t, dt, inv_hyp, 3 counters} (may be null)
   long long plane;    // elements per field plane
   int pitch;          // elements per padded row
   int Nx, Ny;

@@ -502,16 +502,22 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
   const int ite = vs->ite;
   vs->ite = ite + 1;
   if (a.stage == STAGE_EULER) vs->parity = 1 - par;
+  unsigned long long cnt[3];
   for (int k = 0; k < 3; ++k) {
-    vs->counters[k] = atomicAdd(&st->cnt_acc[k], 0ull);
+    cnt[k] = atomicAdd(&st->cnt_acc[k], 0ull);
+    vs->counters[k] = cnt[k];
     st->cnt_acc[k] = 0ull;
   }
   st->acc_hyp = 0ull;
   const int n = vs->steps_in_call;
   if (a.log && n < vs->log_cap) {
-    a.log[3 * n + 0] = t_before;
-    a.log[3 * n + 1] = dt;
-    a.log[3 * n + 2] = inv_prev;
+    double *rec = a.log + 6 * n;
+    rec[0] = t_before;
+    rec[1] = dt;
+    rec[2] = inv_prev;
+    rec[3] = (double)cnt[0];
+    rec[4] = (double)cnt[1];
+    rec[5] = (double)cnt[2];
   }
   vs->steps_in_call = n + 1;
   if (a.driven) {

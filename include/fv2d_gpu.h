@@ -115,9 +115,12 @@ int fv2d_run_async(fv2d_ctx *ctx, int n);
 int fv2d_get_time(fv2d_ctx *ctx, double *t, int *iteration);
 int fv2d_set_time(fv2d_ctx *ctx, double t, int iteration);
 
-/* Per-iteration record of the last fv2d_advance call: for each iteration
- * {t before the update, dt, inv_dt_hyp}; returns the number of records
- * written (at most max_records). */
+/* Per-iteration records of the last fv2d_advance / fv2d_run_async call (the
+ * first 4096 iterations): 6 doubles per iteration, {t before the update, dt,
+ * inv_dt_hyp of the state dt was computed from, negative-density count,
+ * negative-pressure count, NaN count} -- what main.cpp:60-70 and
+ * checkNegatives (SimInfo.h:637-645) print.  *count receives the number of
+ * records written (at most max_records). */
 int fv2d_get_step_log(fv2d_ctx *ctx, double *records, int max_records, int *count);
 
 /* Human-readable message of the last failure on this context (never NULL). */

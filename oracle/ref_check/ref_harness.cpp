@@ -13,6 +13,7 @@
 #include "Update.h"
 
 #include <cstring>
+#include <fstream>
 #include <memory>
 
 using namespace fv2d;
@@ -73,6 +74,35 @@ int fv2d_ref_param(void *h, const char *name, double *out) {
   else if (n == "fslp_K") *out = d.fslp_K;
   else return 1;
   return 0;
+}
+
+// Reader::outputValues of the parsed .ini (SimInfo.h:224-262).
+int fv2d_ref_echo(void *h, const char *out_path) {
+  auto *s = static_cast<RefSim *>(h);
+  std::ofstream out(out_path);
+  s->params.reader.outputValues(out);
+  return out ? 0 : 1;
+}
+
+// Every DeviceParams / Params value the C-ABI parameter block mirrors, in a
+// fixed order (doubles; integers and enums converted).
+int fv2d_ref_dump(void *h, double *out, int n) {
+  auto *s = static_cast<RefSim *>(h);
+  const auto &d = s->params.device_params;
+  const auto &P = s->params;
+  const double v[] = {(double)d.Nx, (double)d.Ny, (double)d.Ng, d.xmin, d.xmax, d.ymin, d.ymax, d.CFL,
+                      (double)d.boundary_x, (double)d.boundary_y, (double)d.reconstruction, (double)d.riemann_solver,
+                      (double)P.time_stepping, P.tend, P.save_freq, d.gamma0, d.epsilon, P.epsilon_reset_negative,
+                      (double)d.well_balanced_flux_at_y_bc, d.fslp_K, (double)P.seed, (double)P.log_frequency,
+                      (double)d.gravity_mode, (double)d.analytical_gravity_mode, d.gx, d.gy, d.hot_bubble_g0,
+                      (double)d.thermal_conductivity_active, (double)d.thermal_conductivity_mode, d.kappa,
+                      (double)d.bctc_ymin, (double)d.bctc_ymax, d.bctc_ymin_value, d.bctc_ymax_value,
+                      (double)d.viscosity_active, (double)d.viscosity_mode, d.mu, d.m1, d.theta1, d.m2, d.theta2,
+                      d.h84_pert, d.c91_pert, d.kh_a, d.kh_amp, d.kh_P0, d.kh_rho_fac, d.kh_sigma, d.kh_uflow, d.kh_y1,
+                      d.kh_y2, d.gresho_density, d.gresho_Mach};
+  const int m = (int)(sizeof(v) / sizeof(v[0]));
+  for (int k = 0; k < m && k < n; ++k) out[k] = v[k];
+  return m;
 }
 
 int fv2d_ref_init(void *h) {

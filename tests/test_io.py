@@ -1,0 +1,232 @@
+"""The .ini parameters and HDF5 snapshot layout (include/fv2d_io.h), no GPU.
+
+* .ini: inih line rules, the Reader's float rounding, map-valued errors; and,
+  where the reference checkout is present, every settings/*.ini read by this
+  library equals the reference's own readInifile result (all parameters) and
+  the echoed parameter file is byte-identical to Reader::outputValues.
+* HDF5: snapshots written by the library are read back by its own reader and
+  by an independent Python reader (tests/h5lite.py); both readers also parse
+  a file written by libhdf5 itself (scipy's MATLAB v7.3 test file).
+"""
+import ctypes as C
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import fv2d_gb300 as fv
+from fv2d_gb300._abi import Params
+from fv2d_testlib import ref_available, ref_lib
+from h5lite import H5
+
+REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+
+
+class RunConfig(C.Structure):
+    _fields_ = [("problem", C.c_char * 64), ("output_filename", C.c_char * 256), ("output_path", C.c_char * 512),
+                ("restart_file", C.c_char * 512), ("multiple_outputs", C.c_int32), ("problem_id", C.c_int32)]
+
+
+def io_lib():
+    L = fv.lib()
+    L.fv2d_read_ini.argtypes = [C.c_char_p, C.POINTER(Params), C.POINTER(RunConfig), C.c_char_p, C.c_int]
+    L.fv2d_write_ini_echo.argtypes = [C.c_char_p, C.c_char_p]
+    L.fv2d_snapshot_write.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(Params), C.c_char_p,
+                                      C.c_int, C.c_double, C.POINTER(C.c_double), C.c_char_p, C.c_int]
+    L.fv2d_snapshot_read.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_int), C.c_char_p, C.c_int]
+    L.fv2d_h5_read_doubles.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.c_int64,
+                                       C.POINTER(C.c_int64)]
+    L.fv2d_h5_read_attr.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_double)]
+    return L
+
+
+@pytest.fixture(scope="module")
+def L():
+    from fv2d_gb300 import build as b
+    b.build()
+    return io_lib()
+
+
+def read_ini(L, path):
+    p, r = Params(), RunConfig()
+    err = C.create_string_buffer(1024)
+    rc = L.fv2d_read_ini(path.encode(), C.byref(p), C.byref(r), err, 1024)
+    return rc, p, r, err.value.decode()
+
+
+def test_ini_rules(L, tmp_path):
+    f = tmp_path / "a.ini"
+    f.write_text("""; comment
+# other comment
+[MESH]
+nx = 48
+Ny : 24   ; inline comment
+xmax=2.0
+[solvers]
+CFL=0.45
+riemann_solver = hll
+reconstruction=plm
+[physics]
+gamma0 = 1.4
+problem = sod_x
+[gravity]
+mode=constant
+gy = -0.1
+[run]
+boundaries_x = periodic
+tend = 0.3
+""")
+    rc, p, r, err = read_ini(L, str(f))
+    assert rc == 0, err
+    assert (p.Nx, p.Ny) == (48, 24)
+    assert p.xmax == 2.0
+    assert p.CFL == float(np.float32(0.45))  # GetFloat goes through strtof
+    assert p.gamma0 == float(np.float32(1.4))
+    assert p.gy == float(np.float32(-0.1))
+    assert p.riemann_solver == fv.HLL and p.reconstruction == fv.PLM and p.gravity_mode == fv.GRAV_CONSTANT
+    assert p.boundary_x == fv.BC_PERIODIC and p.boundary_y == fv.BC_REFLECTING
+    assert r.problem == b"sod_x" and r.problem_id == 0
+    assert p.epsilon == float(np.float32(1e-6))  # default, also float
+
+
+def test_ini_bad_map_value(L, tmp_path):
+    f = tmp_path / "b.ini"
+    f.write_text("[solvers]\nriemann_solver=roe\n")
+    rc, _, _, err = read_ini(L, str(f))
+    assert rc == fv._abi.ERR_INVALID
+    assert err.startswith("bad parameter for riemann_solver") and "allowed values: fslp, hll, hllc" in err
+
+
+REF_DUMP = ["Nx", "Ny", "Nghosts", "xmin", "xmax", "ymin", "ymax", "CFL", "boundary_x", "boundary_y",
+            "reconstruction", "riemann_solver", "time_stepping", "tend", "save_freq", "gamma0", "epsilon",
+            "epsilon_reset_negative", "well_balanced_flux_at_y_bc", "fslp_K", "seed", "log_frequency", "gravity_mode",
+            "analytical_gravity_mode", "gx", "gy", "hot_bubble_g0", "thermal_conductivity_active",
+            "thermal_conductivity_mode", "kappa", "bctc_ymin", "bctc_ymax", "bctc_ymin_value", "bctc_ymax_value",
+            "viscosity_active", "viscosity_mode", "mu", "m1", "theta1", "m2", "theta2", "h84_pert", "c91_pert",
+            "kh_a", "kh_amp", "kh_P0", "kh_rho_fac", "kh_sigma", "kh_uflow", "kh_y1", "kh_y2", "gresho_density",
+            "gresho_Mach"]
+
+
+@pytest.mark.skipif(not ref_available() or not os.path.isdir(os.path.join(REF_DIR, "settings")),
+                    reason="reference checkout / cross-check build not present")
+def test_ini_matches_reference_reader(L, tmp_path):
+    R = ref_lib()
+    R.fv2d_ref_echo.argtypes = [C.c_void_p, C.c_char_p]
+    R.fv2d_ref_dump.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
+    files = sorted(glob.glob(os.path.join(REF_DIR, "settings", "*.ini")))
+    assert len(files) >= 9
+    for path in files:
+        rc, p, r, err = read_ini(L, path)
+        assert rc == 0, (path, err)
+        h = R.fv2d_ref_create(path.encode())
+        assert h
+        vals = (C.c_double * 64)()
+        n = R.fv2d_ref_dump(h, vals, 64)
+        assert n == len(REF_DUMP)
+        for k, name in enumerate(REF_DUMP):
+            assert float(getattr(p, name)) == vals[k], (os.path.basename(path), name, getattr(p, name), vals[k])
+        mine, theirs = tmp_path / "mine.ini", tmp_path / "ref.ini"
+        assert L.fv2d_write_ini_echo(path.encode(), str(mine).encode()) == 0
+        assert R.fv2d_ref_echo(h, str(theirs).encode()) == 0
+        assert mine.read_text() == theirs.read_text(), os.path.basename(path)
+        R.fv2d_ref_destroy(h)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def write(L, d, name, multiple, trunc, p, problem, it, t, q):
+    err = C.create_string_buffer(512)
+    rc = L.fv2d_snapshot_write(str(d).encode(), name.encode(), multiple, trunc, C.byref(p), problem.encode(), it, t,
+                               _dp(q), err, 512)
+    assert rc == 0, err.value
+
+
+def read(L, file, nx, ny):
+    q = np.empty((ny, nx, 4))
+    t, it = C.c_double(), C.c_int()
+    err = C.create_string_buffer(512)
+    rc = L.fv2d_snapshot_read(file.encode(), nx, ny, _dp(q), C.byref(t), C.byref(it), err, 512)
+    return rc, q, t.value, it.value, err.value.decode()
+
+
+def test_unique_file_roundtrip(L, tmp_path):
+    nx, ny = 12, 7
+    p = fv.default_params(Nx=nx, Ny=ny, xmin=-0.5, xmax=0.7, ymin=0.1, ymax=0.45)
+    rng = np.random.default_rng(3)
+    qs = [rng.uniform(0.1, 2.0, (ny, nx, 4)) for _ in range(3)]
+    times = [0.0, 0.0125, 0.25]
+    for k in range(3):
+        write(L, tmp_path, "run", 0, 1 if k == 0 else 0, p, "blast", k, times[k], qs[k])
+    f = str(tmp_path / "run.h5")
+    # this library's reader: the latest group, then each group by name
+    rc, q, t, it, err = read(L, f, nx, ny)
+    assert rc == 0, err
+    assert it == 2 and t == 0.25 and np.array_equal(q, qs[2])
+    for k in range(3):
+        rc, q, t, it, _ = read(L, f + ":/ite_%04d" % k, nx, ny)
+        assert rc == 0 and it == k and t == times[k] and np.array_equal(q, qs[k])
+    rc, _, _, _, err = read(L, f, nx + 1, ny)
+    assert rc != 0 and "different resolution" in err
+    # independent reader
+    h = H5(f)
+    assert sorted(h.links(h.root)) == ["ite_0000", "ite_0001", "ite_0002", "x", "y"]
+    ra = h.attrs("/")
+    assert (ra["Ntx"], ra["Nty"], ra["Nx"], ra["Ny"], ra["ibeg"], ra["iend"], ra["jbeg"], ra["jend"]) == \
+        (nx + 4, ny + 4, nx, ny, 2, nx + 2, 2, ny + 2)
+    assert ra["problem"].split(b"\0")[0] == b"blast"
+    x, y = h.dataset("/x"), h.dataset("/y")
+    assert x.shape == ((nx + 1) * (ny + 1),)
+    dx = (0.7 - -0.5) / nx
+    assert x[1] == 1 * dx + -0.5 and y[nx + 1] == 1 * ((0.45 - 0.1) / ny) + 0.1
+    for k in range(3):
+        g = "/ite_%04d/" % k
+        a = h.attrs(g)
+        assert a["time"] == times[k] and a["iteration"] == k
+        for f_, name in enumerate(["rho", "u", "v", "prs"]):
+            assert np.array_equal(h.dataset(g + name), qs[k][..., f_].ravel())
+    assert h.eof == os.path.getsize(f)
+    xmf = (tmp_path / "run.xmf").read_text()
+    assert xmf.count("<Grid Name=\"ite_") == 3 and xmf.rstrip().endswith("</Xdmf>")
+    assert "&file;/ite_0002/rho" in xmf
+
+
+def test_multiple_output_files(L, tmp_path):
+    nx, ny = 5, 9
+    p = fv.default_params(Nx=nx, Ny=ny)
+    q = np.random.default_rng(4).uniform(0.5, 1.5, (ny, nx, 4))
+    write(L, tmp_path, "snap", 1, 1, p, "sod_x", 7, 0.5, q)
+    f = str(tmp_path / "snap_0007.h5")
+    rc, q2, t, it, err = read(L, f, nx, ny)
+    assert rc == 0, err
+    assert t == 0.5 and it == 7 and np.array_equal(q, q2)
+    h = H5(f)
+    assert sorted(h.links(h.root)) == ["prs", "rho", "u", "v", "x", "y"]
+    assert h.attrs("/")["iteration"] == 7
+    assert (tmp_path / "snap_0007.xmf").exists()
+
+
+def _matlab_file():
+    try:
+        import scipy
+    except ImportError:
+        return None
+    f = os.path.join(os.path.dirname(scipy.__file__), "io", "matlab", "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    return f if os.path.exists(f) else None
+
+
+@pytest.mark.skipif(_matlab_file() is None, reason="no libhdf5-written file available")
+def test_readers_parse_a_libhdf5_file(L):
+    """A file written by libhdf5 (512-byte user block, superblock v0,
+    symbol-table groups): both readers recover the same dataset."""
+    f = _matlab_file()
+    h = H5(f)
+    ref = h.dataset("/testdouble").ravel()
+    assert np.allclose(ref, np.linspace(0, 2 * np.pi, 9))
+    n = C.c_int64()
+    out = np.empty(64)
+    assert L.fv2d_h5_read_doubles(f.encode(), b"/testdouble", _dp(out), 64, C.byref(n)) == 0
+    assert n.value == 9 and np.array_equal(out[:9], ref)
