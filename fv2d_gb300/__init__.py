@@ -69,6 +69,7 @@ def lib():
         L.fv2d_run_async.argtypes = [vp, C.c_int]
         L.fv2d_probe_fp64_peak.argtypes = [C.c_int, _dp]
         L.fv2d_compute_dt_noalloc.argtypes = [C.POINTER(Params), vp, vp, vp]
+        L.fv2d_selftest_arith.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64), _dp]
         _lib = L
     return _lib
 
@@ -95,6 +96,18 @@ def probe_fp64_peak(device=0):
     if rc != 0:
         raise Fv2dError(rc, "fp64 probe failed")
     return g.value
+
+
+def selftest_arith(op, n, seed=1):
+    """Bit-for-bit check of the integer-pipe binary64 division (op 0) or
+    square root (op 1) against the hardware on n generated operand sets;
+    returns (mismatches, first mismatching {a, b, result})."""
+    bad = C.c_uint64()
+    ex = (C.c_double * 3)()
+    rc = lib().fv2d_selftest_arith(int(op), int(n), int(seed), C.byref(bad), ex)
+    if rc != 0:
+        raise Fv2dError(rc, "self-test failed to run")
+    return bad.value, list(ex)
 
 
 NOALLOC_MAX_CELLS = 4096 * 4096

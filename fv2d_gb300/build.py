@@ -41,6 +41,7 @@ UNITS = [
     ("step_hllc.cu", ["-fmad=false"]),
     ("step_fslp.cu", ["-fmad=false"]),
     ("probe.cu", []),
+    ("selftest.cu", ["-fmad=false"]),
     ("noalloc.cu", ["-fmad=false"]),
     ("batch_kernels.cu", ["-use_fast_math"]),
     ("serve.cu", []),

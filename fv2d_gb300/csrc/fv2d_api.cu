@@ -96,7 +96,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 // ------------------------------------------------------------------ kernels
 __device__ __forceinline__ double ddiv_c(double x, double d, double inv_d, int pow2) {
-  return pow2 ? x * inv_d : x / d;
+  return pow2 ? x * inv_d : fv_div(x, d);
 }
 
 // Set-up pass: interleaved interior primitives -> planes, every ghost cell

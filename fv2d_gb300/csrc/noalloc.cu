@@ -57,7 +57,7 @@ struct DtArgs {
 };
 
 __device__ __forceinline__ double div_spacing(double x, double d, double inv_d, int pow2) {
-  return pow2 ? x * inv_d : x / d;
+  return pow2 ? x * inv_d : fv2d::fv_div(x, d);
 }
 
 // Same per-cell expression and the same max semantics as the dt reduction of

@@ -17,7 +17,29 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "softfp.cuh"
+
 namespace fv2d {
+
+// Division and square root: binary64 on the device goes through the
+// integer-pipe routines (same correctly rounded bits as the hardware
+// instructions, off the FP64 pipe); binary32 and host code use the operators.
+__host__ __device__ __forceinline__ double fv_div(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return softfp::div_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+__host__ __device__ __forceinline__ float fv_div(float a, float b) { return a / b; }
+__host__ __device__ __forceinline__ double fv_sqrt(double x) {
+#ifdef __CUDA_ARCH__
+  return softfp::sqrt_rn(x);
+#else
+  return sqrt(x);
+#endif
+}
+__host__ __device__ __forceinline__ float fv_sqrt(float x) { return sqrtf(x); }
 
 enum { IR = 0, IU = 1, IV = 2, IP = 3, IE = 3 };
 
@@ -42,8 +64,8 @@ __host__ __device__ __forceinline__ S4<R> prim_to_cons(const S4<R> &q, const Gas
   s.r = q.r;
   s.u = q.r * q.u;
   s.v = q.r * q.v;
-  R Ek = R(0.5) * (s.u * s.u + s.v * s.v) / q.r;
-  s.p = (Ek + q.p / g.gm1);
+  R Ek = fv_div(R(0.5) * (s.u * s.u + s.v * s.v), q.r);
+  s.p = (Ek + fv_div(q.p, g.gm1));
   return s;
 }
 
@@ -52,8 +74,8 @@ template <class R>
 __host__ __device__ __forceinline__ S4<R> cons_to_prim(const S4<R> &u, const Gas<R> &g) {
   S4<R> q;
   q.r = u.r;
-  q.u = u.u / u.r;
-  q.v = u.v / u.r;
+  q.u = fv_div(u.u, u.r);
+  q.v = fv_div(u.v, u.r);
   R Ek = R(0.5) * q.r * (q.u * q.u + q.v * q.v);
   q.p = (u.p - Ek) * g.gm1;
   return q;
@@ -61,13 +83,13 @@ __host__ __device__ __forceinline__ S4<R> cons_to_prim(const S4<R> &u, const Gas
 
 template <class R>
 __device__ __forceinline__ R dsqrt(R x) {
-  return sqrt(x);
+  return fv_sqrt(x);
 }
 
 // States.h:45-46
 template <class R>
 __device__ __forceinline__ R sound_speed(const S4<R> &q, const Gas<R> &g) {
-  return dsqrt(q.p * g.gamma / q.r);
+  return dsqrt(fv_div(q.p * g.gamma, q.r));
 }
 
 // Update.h:77-85
@@ -96,8 +118,8 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   const R SR = fmax(smaxL, smaxR);
   // computeFlux (RiemannSolvers.h:133-141).  p/(gamma-1) is also the pressure
   // term of primToCons below: the same division, evaluated once.
-  const R peL = qL.p / g.gm1;
-  const R peR = qR.p / g.gm1;
+  const R peL = fv_div(qL.p, g.gm1);
+  const R peR = fv_div(qR.p, g.gm1);
   const R EkL = R(0.5) * qL.r * (qL.u * qL.u + qL.v * qL.v);
   const R EkR = R(0.5) * qR.r * (qR.u * qR.u + qR.v * qR.v);
   const R EL = (peL + EkL);
@@ -107,15 +129,15 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   S4<R> FR{ruR, ruR * qR.u + qR.p, ruR * qR.v, (qR.p + ER) * qR.u};
   // primToCons (States.h:19-30) of both states
   const R mvL = qL.r * qL.v, mvR = qR.r * qR.v;
-  const R uEL = (R(0.5) * (ruL * ruL + mvL * mvL) / qL.r + peL);
-  const R uER = (R(0.5) * (ruR * ruR + mvR * mvR) / qR.r + peR);
+  const R uEL = (fv_div(R(0.5) * (ruL * ruL + mvL * mvL), qL.r) + peL);
+  const R uER = (fv_div(R(0.5) * (ruR * ruR + mvR * mvR), qR.r) + peR);
   const R SLSR = SL * SR;
   const R den = SR - SL;
   S4<R> FM;
-  FM.r = (SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r)) / den;
-  FM.u = (SR * FL.u - SL * FR.u + SLSR * (ruR - ruL)) / den;
-  FM.v = (SR * FL.v - SL * FR.v + SLSR * (mvR - mvL)) / den;
-  FM.p = (SR * FL.p - SL * FR.p + SLSR * (uER - uEL)) / den;
+  FM.r = fv_div(SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r), den);
+  FM.u = fv_div(SR * FL.u - SL * FR.u + SLSR * (ruR - ruL), den);
+  FM.v = fv_div(SR * FL.v - SL * FR.v + SLSR * (mvR - mvL), den);
+  FM.p = fv_div(SR * FL.p - SL * FR.p + SLSR * (uER - uEL), den);
   const R pM = R(0.5) * (qL.p + qR.p);
   const bool left = (SL >= R(0));
   const bool right = !left && (SR <= R(0));
@@ -144,16 +166,16 @@ __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S
   const R SR = fmax(uL, uR) + cmax;
   const R rcL = rL * (uL - SL);
   const R rcR = rR * (SR - uR);
-  const R uS = (rcR * uR + rcL * uL + (pL - pR)) / (rcR + rcL);
-  const R pS = (rcR * pL + rcL * pR + rcL * rcR * (uL - uR)) / (rcR + rcL);
+  const R uS = fv_div(rcR * uR + rcL * uL + (pL - pR), rcR + rcL);
+  const R pS = fv_div(rcR * pL + rcL * pR + rcL * rcR * (uL - uR), rcR + rcL);
   const bool sideL = (uS > R(0));
   const R rK = sideL ? rL : rR;
   const R uK = sideL ? uL : uR;
   const R pK = sideL ? pL : pR;
   const R EK = sideL ? EL : ER;
   const R SK = sideL ? SL : SR;
-  const R rS = rK * (SK - uK) / (SK - uS);
-  const R ES = ((SK - uK) * EK - pK * uK + pS * uS) / (SK - uS);
+  const R rS = fv_div(rK * (SK - uK), SK - uS);
+  const R ES = fv_div((SK - uK) * EK - pK * uK + pS * uS, SK - uS);
   // branch order of RiemannSolvers.h:89-112
   const bool bL = (SL > R(0));
   const bool bStar = !bL && (sideL || SR > R(0));
@@ -177,15 +199,15 @@ template <class R>
 __device__ __forceinline__ void riemann_fslp(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, R gdx,
                                              const Gas<R> &g) {
   const R rhoL = qL.r, uL = qL.u, pL = qL.p;
-  const R csL = dsqrt(g.gamma * pL / rhoL);
+  const R csL = dsqrt(fv_div(g.gamma * pL, rhoL));
   const R rhoR = qR.r, uR = qR.u, pR = qR.p;
-  const R csR = dsqrt(g.gamma * pR / rhoR);
+  const R csR = dsqrt(fv_div(g.gamma * pR, rhoR));
   const R zL = rhoL * csL, zR = rhoR * csR;
   const R ai = g.fslp_K * ((zL < zR) ? zR : zL);
-  const R mL = fabs(uL) / csL, mR = fabs(uR) / csR;
+  const R mL = fv_div(fabs(uL), csL), mR = fv_div(fabs(uR), csR);
   const R mx = (mL < mR) ? mR : mL;
   const R theta = (mx < R(1)) ? mx : R(1);
-  const R ustar = R(0.5) * (uR + uL) - R(0.5) / ai * (pR - pL - R(0.5) * (rhoL + rhoR) * gdx);
+  const R ustar = R(0.5) * (uR + uL) - fv_div(R(0.5), ai) * (pR - pL - R(0.5) * (rhoL + rhoR) * gdx);
   const R Pi = R(0.5) * (pR + pL) - theta * R(0.5) * ai * (uR - uL);
   const bool up = ustar > R(0);
   const R sr = up ? qL.r : qR.r;
@@ -193,7 +215,7 @@ __device__ __forceinline__ void riemann_fslp(const S4<R> &qL, const S4<R> &qR, S
   const R sv = up ? qL.v : qR.v;
   const R sp = up ? qL.p : qR.p;
   const R Ekstar = R(0.5) * sr * (su * su + sv * sv);
-  const R Estar = Ekstar + sp / g.gm1;
+  const R Estar = Ekstar + fv_div(sp, g.gm1);
   f.r = ustar * sr;
   f.u = ustar * sr * su + Pi;
   f.v = ustar * sr * sv;
@@ -221,8 +243,8 @@ __host__ __device__ __forceinline__ S4<R> hancock(const S4<R> &q, const S4<R> &s
                                                   R gamma) {
   S4<R> h;
   h.r = q.r - (ax * (q.u * sx.r + q.r * sx.u) + ay * (q.v * sy.r + q.r * sy.v));
-  h.u = q.u - (ax * (q.u * sx.u + sx.p / q.r) + ay * (q.v * sy.u));
-  h.v = q.v - (ax * (q.u * sx.v) + ay * (q.v * sy.v + sy.p / q.r));
+  h.u = q.u - (ax * (q.u * sx.u + fv_div(sx.p, q.r)) + ay * (q.v * sy.u));
+  h.v = q.v - (ax * (q.u * sx.v) + ay * (q.v * sy.v + fv_div(sy.p, q.r)));
   h.p = q.p - (ax * (gamma * q.p * sx.u + q.u * sx.p) + ay * (gamma * q.p * sy.v + q.v * sy.p));
   return h;
 }

@@ -1,0 +1,99 @@
+// selftest.cu -- checks the integer-pipe binary64 division and square root
+// (softfp.cuh) bit for bit against the hardware instructions on this GPU.
+#include <cuda_runtime.h>
+
+#include "../../include/fv2d_gpu.h"
+#include "softfp.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix(uint64_t z) {  // SplitMix64 finaliser
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// Operand of class `mode` from a 64-bit random word:
+//  0: random significand, exponent in [-60, 60]      1: any bit pattern
+//  2: significand with few set bits (exact quotients, ties, perfect squares)
+//  3: exponent near the overflow/underflow limits
+__device__ __forceinline__ double operand(uint64_t r, uint64_t r2, int mode) {
+  uint64_t bits;
+  switch (mode) {
+    case 0: bits = (r & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 60 + (int)(r2 % 121)) << 52); break;
+    case 1: bits = r; break;
+    case 2: bits = (r & 0x800FF00000000000ull) | ((uint64_t)(1023 - 8 + (int)(r2 % 17)) << 52); break;
+    default: {
+      const int e = (r2 & 1) ? 1 + (int)(r2 % 40) : 2046 - (int)(r2 % 40);
+      bits = (r & 0x800FFFFFFFFFFFFFull) | ((uint64_t)e << 52);
+    }
+  }
+  return __longlong_as_double((long long)bits);
+}
+
+__global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long long *bad, double *ex) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t r0 = mix(seed ^ (i * 4)), r1 = mix(seed ^ (i * 4 + 1)), r2 = mix(seed ^ (i * 4 + 2)),
+                   r3 = mix(seed ^ (i * 4 + 3));
+    const int mode = (int)(r3 & 3);
+    double a = operand(r0, r2, mode), b = operand(r1, r3 >> 8, mode);
+    if (op == 0 && mode == 2 && (r3 & 4)) {  // a = b * k +- 1 ulp: quotients next to representable values
+      const double k = operand(r2, r0, 2);
+      a = b * k;
+      a = __longlong_as_double(__double_as_longlong(a) + ((r3 & 8) ? 1 : -1));
+    }
+    if (op == 1 && mode == 2 && (r3 & 4)) {  // perfect squares +- 1 ulp
+      a = b * b;
+      a = __longlong_as_double(__double_as_longlong(a) + ((r3 & 8) ? 1 : ((r3 & 16) ? 0 : -1)));
+    }
+    double h, s;
+    if (op == 0) {
+      h = a / b;
+      s = fv2d::softfp::div_rn(a, b);
+    } else {
+      a = fabs(a);
+      h = sqrt(a);
+      s = fv2d::softfp::sqrt_rn(a);
+    }
+    const bool same = __double_as_longlong(h) == __double_as_longlong(s) || (h != h && s != s);
+    if (!same) {
+      const unsigned long long k = atomicAdd(bad, 1ull);
+      if (k == 0) {
+        ex[0] = a;
+        ex[1] = b;
+        ex[2] = s;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int fv2d_selftest_arith(int op, uint64_t n, uint64_t seed, uint64_t *mismatches, double example[3]) {
+  if ((op != 0 && op != 1) || !mismatches) return FV2D_ERR_INVALID;
+  unsigned long long *bad = nullptr;
+  double *ex = nullptr;
+  if (cudaMalloc(&bad, sizeof(*bad)) != cudaSuccess || cudaMalloc(&ex, 3 * sizeof(double)) != cudaSuccess) {
+    cudaFree(bad);
+    return FV2D_ERR_NOMEM;
+  }
+  cudaMemset(bad, 0, sizeof(*bad));
+  cudaMemset(ex, 0, 3 * sizeof(double));
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  selftest_kernel<<<sms * 8, 256>>>(op, n, seed, bad, ex);
+  unsigned long long h = 0;
+  double hx[3] = {0, 0, 0};
+  const cudaError_t e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaMemcpy(hx, ex, sizeof(hx), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  cudaFree(ex);
+  if (e != cudaSuccess) return FV2D_ERR_CUDA;
+  *mismatches = h;
+  if (example)
+    for (int k = 0; k < 3; ++k) example[k] = hx[k];
+  return FV2D_OK;
+}

@@ -1,0 +1,145 @@
+// softfp.cuh -- correctly rounded binary64 division and square root computed
+// on the integer and FP32 pipes.
+//
+// GB300 executes binary64 at 1/64 of its FP32 rate; a hardware double
+// division or square root occupies that pipe for ~7-8 DFMA-equivalents while
+// the integer pipes stay idle in the FP64 step kernel.  These routines return
+// exactly the IEEE round-to-nearest-even result (the same bits as x / y and
+// sqrt(x)) for finite normal operands with a normal result, and defer every
+// other case (zeros, subnormals, infinities, NaNs, overflow, underflow) to the
+// hardware instruction.
+//
+// Division: the divisor's 53-bit significand is normalised to a 64-bit word d;
+// its reciprocal word v = floor((2^128 - 1) / d) - 2^64 (the definition of
+// Moller & Granlund, "Improved division by invariant integers", IEEE TC 2011)
+// is seeded from the FP32 reciprocal, refined by two Newton-Raphson steps in
+// 64-bit fixed point and made exact by a final check; their 2-by-1 division
+// step then yields the exact 53-bit quotient and remainder, from which the
+// rounding is decided (compare twice the remainder with the divisor).
+//
+// Square root: the FP32 reciprocal square root seeds a Newton-Raphson
+// iteration for 1/sqrt in 64-bit fixed point; the product with the operand
+// gives the integer square root within a few units, which the exact remainder
+// M - S^2 corrects; round up when the remainder exceeds S.
+#pragma once
+
+#include <stdint.h>
+
+namespace fv2d {
+namespace softfp {
+
+__device__ __forceinline__ uint64_t recip_word(uint64_t d) {
+  const float df = __ull2float_rz(d >> 40);  // in [2^23, 2^24)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(df));
+  const float y = r * 16777216.0f;  // ~2^24/df, in (1, 2]
+  uint64_t x = __float2ull_rz((y - 1.0f) * 18446744073709551616.0f);
+  for (int it = 0; it < 2; ++it) {
+    // e = 2^128 - d (2^64 + x); x += (2^64 + x) e / 2^128
+    const uint64_t lo = d * x, hi = __umul64hi(d, x);
+    const uint64_t s_hi = hi + d;
+    const int64_t e_hi = (int64_t)(0ull - s_hi - (lo != 0));
+    const int64_t corr = e_hi + (int64_t)(__umul64hi(x, (uint64_t)e_hi) - (e_hi < 0 ? x : 0ull));
+    x += (uint64_t)corr;
+  }
+  // exact: d (2^64 + x) <= 2^128 - 1 < d (2^64 + x + 1)
+#pragma unroll 1
+  for (int k = 0; k < 4; ++k) {
+    const uint64_t lo = d * x, hi = __umul64hi(d, x);
+    const uint64_t s_hi = hi + d;
+    if (s_hi < d) {
+      --x;
+      continue;
+    }
+    const uint64_t lo2 = lo + d;
+    const uint64_t s_hi2 = s_hi + (lo2 < lo);
+    if (s_hi2 < s_hi) break;
+    ++x;
+  }
+  return x;
+}
+
+// a / b, round to nearest even.
+__device__ __forceinline__ double div_rn(double a, double b) {
+  const uint64_t ia = (uint64_t)__double_as_longlong(a), ib = (uint64_t)__double_as_longlong(b);
+  const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
+  const uint64_t ma = (ia & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const uint64_t mb = (ib & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const bool big = ma >= mb;
+  int e = ea - eb + 1023 - (big ? 0 : 1);
+  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || e <= 0 || e >= 0x7fe) return a / b;
+  // Q = floor(n 2^52 / mb) with n = ma or 2 ma, i.e. (n 2^63) / (mb 2^11)
+  const uint64_t d = mb << 11;
+  const uint64_t n = big ? ma : (ma << 1);
+  const uint64_t u1 = n >> 1, u0 = n << 63;
+  const uint64_t v = recip_word(d);
+  uint64_t q0 = v * u1, q1 = __umul64hi(v, u1);
+  const uint64_t s0 = q0 + u0;
+  q1 = q1 + u1 + (s0 < q0) + 1;
+  q0 = s0;
+  uint64_t r = u0 - q1 * d;
+  if (r > q0) {
+    --q1;
+    r += d;
+  }
+  if (r >= d) {
+    ++q1;
+    r -= d;
+  }
+  // nearest even: compare 2 r with d
+  uint64_t Q = q1 + ((r > d - r) || (r == d - r && (q1 & 1)));
+  if (Q >> 53) {
+    Q >>= 1;
+    ++e;
+  }
+  const uint64_t bits = ((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull) | ((ia ^ ib) & 0x8000000000000000ull);
+  return __longlong_as_double((long long)bits);
+}
+
+// sqrt(x), round to nearest even.
+__device__ __forceinline__ double sqrt_rn(double x) {
+  const uint64_t ix = (uint64_t)__double_as_longlong(x);
+  const int E = (int)(ix >> 52);  // sign bit included: negative values fail the range test
+  if (E == 0 || E >= 0x7ff) return sqrt(x);
+  const uint64_t m = (ix & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int t = E - 1075;  // x = m 2^t
+  const int odd = t & 1;
+  // M = m 2^(52 + odd) in [2^104, 2^106); S = floor(sqrt(M)) in [2^52, 2^53)
+  const uint64_t Z = m << (10 + odd);  // M / 2^42, in [2^62, 2^64)
+  // Y ~ 2^94 / sqrt(Z), in (2^62, 2^63]
+  const float zf = __ull2float_rz(Z >> 40);  // Z / 2^40
+  float rs;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rs) : "f"(zf));
+  uint64_t Y = __float2ull_rz(rs * 0x1p74f);  // rs = 2^20 / sqrt(Z)
+  for (int it = 0; it < 2; ++it) {
+    // U = Z Y^2 / 2^128 ~ 2^60; Y <- Y (3 2^60 - U) / 2^61
+    const uint64_t W = __umul64hi(Y, Y);
+    const uint64_t U = __umul64hi(Z, W);
+    Y = __umul64hi(Y, (0x3000000000000000ull - U) << 2) << 1;
+  }
+  // sqrt(M) = sqrt(Z) 2^21 = Z Y / 2^73
+  uint64_t S = __umul64hi(Z, Y) >> 9;
+  // exact remainder R = M - S^2 (small; the low 64 bits carry it)
+  const uint64_t Mlo = m << (52 + odd);
+  int64_t R = (int64_t)(Mlo - S * S);
+#pragma unroll 1
+  for (int k = 0; k < 4 && R < 0; ++k) {
+    R += (int64_t)(2 * S - 1);
+    --S;
+  }
+#pragma unroll 1
+  for (int k = 0; k < 4 && R > (int64_t)(2 * S); ++k) {
+    R -= (int64_t)(2 * S + 1);
+    ++S;
+  }
+  uint64_t Q = S + (R > (int64_t)S);
+  int e = ((t - odd) >> 1) + 26 + 1023;  // sqrt(x) = Q 2^((t - odd)/2 - 26), Q in [2^52, 2^53]
+  if (Q >> 53) {
+    Q >>= 1;
+    ++e;
+  }
+  return __longlong_as_double((long long)(((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull)));
+}
+
+}  // namespace softfp
+}  // namespace fv2d

@@ -78,7 +78,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err_flag) 
 __device__ __forceinline__ double ddivc(double x, double d, double inv_d, int pow2) {
   // x / d; when 1/d is exactly representable the product is the same
   // correctly rounded value.
-  return pow2 ? x * inv_d : x / d;
+  return pow2 ? x * inv_d : fv_div(x, d);
 }
 
 __device__ __forceinline__ double warp_max_nonneg(double v) {
@@ -187,12 +187,12 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
   if (a.tc) {
     for (int it = tid; it < L::R1; it += NT) {
       const int ly = it / L::R1W + 1, lx = it % L::R1W + 1;
-      sR1(L::T, 0, ly, lx) = sQ(3, ly, lx) / sQ(0, ly, lx);
+      sR1(L::T, 0, ly, lx) = fv_div(sQ(3, ly, lx), sQ(0, ly, lx));
     }
   }
   __syncthreads();
   if constexpr (RECON == RECON_MH) {
-    const double ax = 0.5 * dt / a.dx, ay = 0.5 * dt / a.dy;
+    const double ax = fv_div(0.5 * dt, a.dx), ay = fv_div(0.5 * dt, a.dy);
     for (int it = tid; it < L::R1; it += NT) {
       const int ly = it / L::R1W + 1, lx = it % L::R1W + 1;
       S4<double> sx{sR1(L::SX, 0, ly, lx), sR1(L::SX, 1, ly, lx), sR1(L::SX, 2, ly, lx), sR1(L::SX, 3, ly, lx)};
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
         else
           FRt = kR * a.bctc_ymax_value;
       }
-      const double dtdx = dt / a.dx, dtdy = dt / a.dy;
+      const double dtdx = fv_div(dt, a.dx), dtdy = fv_div(dt, a.dy);
       un[3] += dtdx * (FRt - FLt) + dtdy * (FDt - FUt);
     }
     // viscosity (Viscosity.h:148-228)

@@ -159,6 +159,14 @@ int fv2d_probe_fp64_peak(int device, double *gflops);
 #define FV2D_NOALLOC_MAX_CELLS (4096 * 4096)
 int fv2d_compute_dt_noalloc(const fv2d_params *p, const double *q_dev, double *out_dev, void *stream);
 
+/* Self-test of the step kernel's binary64 arithmetic on the integer pipes:
+ * op 0 = division, 1 = square root.  Evaluates n generated operand sets
+ * (random significands, arbitrary bit patterns, near-tie and exact cases,
+ * extreme exponents) with both the integer routine and the hardware
+ * instruction and counts results whose bits differ (NaNs compare equal).
+ * example receives {a, b, integer result} of the first mismatch. */
+int fv2d_selftest_arith(int op, uint64_t n, uint64_t seed, uint64_t *mismatches, double example[3]);
+
 /* sizeof(fv2d_params) as compiled into the library. */
 size_t fv2d_params_size(void);
 
