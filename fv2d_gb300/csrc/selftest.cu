@@ -18,15 +18,22 @@ __device__ __forceinline__ uint64_t mix(uint64_t z) {  // SplitMix64 finaliser
 //  0: random significand, exponent in [-60, 60]      1: any bit pattern
 //  2: significand with few set bits (exact quotients, ties, perfect squares)
 //  3: exponent near the overflow/underflow limits
+//  4: significand within 4096 ulps above or below a power of two (the
+//     divisor's reciprocal word is then near 2^64 - 1 or near 0)
 __device__ __forceinline__ double operand(uint64_t r, uint64_t r2, int mode) {
   uint64_t bits;
   switch (mode) {
     case 0: bits = (r & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 60 + (int)(r2 % 121)) << 52); break;
     case 1: bits = r; break;
     case 2: bits = (r & 0x800FF00000000000ull) | ((uint64_t)(1023 - 8 + (int)(r2 % 17)) << 52); break;
-    default: {
+    case 3: {
       const int e = (r2 & 1) ? 1 + (int)(r2 % 40) : 2046 - (int)(r2 % 40);
       bits = (r & 0x800FFFFFFFFFFFFFull) | ((uint64_t)e << 52);
+      break;
+    }
+    default: {
+      const uint64_t small = r & 0xFFFull, frac = (r2 & 1) ? small : 0xFFFFFFFFFFFFFull - small;
+      bits = (r & 0x8000000000000000ull) | frac | ((uint64_t)(1023 - 8 + (int)((r2 >> 1) % 17)) << 52);
     }
   }
   return __longlong_as_double((long long)bits);
@@ -37,7 +44,7 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t r0 = mix(seed ^ (i * 4)), r1 = mix(seed ^ (i * 4 + 1)), r2 = mix(seed ^ (i * 4 + 2)),
                    r3 = mix(seed ^ (i * 4 + 3));
-    const int mode = (int)(r3 & 3);
+    const int mode = (int)((r3 >> 32) % 5);
     double a = operand(r0, r2, mode), b = operand(r1, r3 >> 8, mode);
     if (op == 0 && mode == 2 && (r3 & 4)) {  // a = b * k +- 1 ulp: quotients next to representable values
       const double k = operand(r2, r0, 2);

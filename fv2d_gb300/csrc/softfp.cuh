@@ -40,7 +40,12 @@ __device__ __forceinline__ uint64_t recip_word(uint64_t d) {
     const uint64_t s_hi = hi + d;
     const int64_t e_hi = (int64_t)(0ull - s_hi - (lo != 0));
     const int64_t corr = e_hi + (int64_t)(__umul64hi(x, (uint64_t)e_hi) - (e_hi < 0 ? x : 0ull));
-    x += (uint64_t)corr;
+    // A Newton step from an overestimate lands below the root by about the
+    // squared error (2^-46 relative after the FP32 seed).  For a divisor
+    // just below a power of two (d > 2^64 - 2^19) the root v is smaller than
+    // that and the step would cross 2^64 + 0, wrapping the fraction word:
+    // clamp at zero, an underestimate the next step refines.
+    x = (corr < 0 && (uint64_t)(-corr) > x) ? 0ull : x + (uint64_t)corr;
   }
   // exact: d (2^64 + x) <= 2^128 - 1 < d (2^64 + x + 1)
 #pragma unroll 1
