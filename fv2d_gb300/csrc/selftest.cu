@@ -55,6 +55,8 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
       a = b * b;
       a = __longlong_as_double(__double_as_longlong(a) + ((r3 & 8) ? 1 : ((r3 & 16) ? 0 : -1)));
     }
+    if (((r3 >> 20) & 15) == 0) a = copysign(0.0, a);  // zero dividends / radicands
+    if (((r3 >> 24) & 63) == 0) b = copysign(0.0, b);  // division by zero
     double h, s;
     if (op == 0) {
       h = a / b;

@@ -5,9 +5,10 @@
 // division or square root occupies that pipe for ~7-8 DFMA-equivalents while
 // the integer pipes stay idle in the FP64 step kernel.  These routines return
 // exactly the IEEE round-to-nearest-even result (the same bits as x / y and
-// sqrt(x)) for finite normal operands with a normal result, and defer every
-// other case (zeros, subnormals, infinities, NaNs, overflow, underflow) to the
-// hardware instruction.
+// sqrt(x)) for finite normal operands with a normal result and for zero
+// dividends and radicands, and defer every other case (subnormals,
+// infinities, NaNs, division by zero, overflow, underflow) to the hardware
+// instruction.
 //
 // Division: the divisor's 53-bit significand is normalised to a 64-bit word d;
 // its reciprocal word v = floor((2^128 - 1) / d) - 2^64 (the definition of
@@ -28,12 +29,17 @@
 namespace fv2d {
 namespace softfp {
 
+// The seeds are assembled from bit fields rather than by int64 <-> float
+// conversions, which issue on the binary64 pipe.
 __device__ __forceinline__ uint64_t recip_word(uint64_t d) {
-  const float df = __ull2float_rz(d >> 40);  // in [2^23, 2^24)
+  // f = d / 2^63 truncated to 24 bits, in [1, 2); r ~ 1/f in (1/2, 1]
+  const float f = __uint_as_float(0x3F800000u | ((uint32_t)(d >> 40) & 0x7FFFFFu));
   float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(df));
-  const float y = r * 16777216.0f;  // ~2^24/df, in (1, 2]
-  uint64_t x = __float2ull_rz((y - 1.0f) * 18446744073709551616.0f);
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
+  // x = (2 r - 1) 2^64: the fraction field of 2 r shifted up, clamped to
+  // [0, 2^64 - 1] when the approximation leaves [1/2, 1)
+  const uint32_t rb = __float_as_uint(r);
+  uint64_t x = rb >= 0x3F800000u ? ~0ull : rb < 0x3F000000u ? 0ull : (uint64_t)(rb & 0x7FFFFFu) << 41;
   for (int it = 0; it < 2; ++it) {
     // e = 2^128 - d (2^64 + x); x += (2^64 + x) e / 2^128
     const uint64_t lo = d * x, hi = __umul64hi(d, x);
@@ -72,7 +78,13 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   const uint64_t mb = (ib & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   const bool big = ma >= mb;
   int e = ea - eb + 1023 - (big ? 0 : 1);
-  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || e <= 0 || e >= 0x7fe) return a / b;
+  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || e <= 0 || e >= 0x7fe) {
+    // +-0 / (finite nonzero normal) is a zero with the xor of the signs;
+    // quiescent regions (zero momentum) make this the common special case.
+    if ((ia << 1) == 0 && eb != 0 && eb != 0x7ff)
+      return __longlong_as_double((long long)((ia ^ ib) & 0x8000000000000000ull));
+    return a / b;
+  }
   // Q = floor(n 2^52 / mb) with n = ma or 2 ma, i.e. (n 2^63) / (mb 2^11)
   const uint64_t d = mb << 11;
   const uint64_t n = big ? ma : (ma << 1);
@@ -105,17 +117,20 @@ __device__ __forceinline__ double div_rn(double a, double b) {
 __device__ __forceinline__ double sqrt_rn(double x) {
   const uint64_t ix = (uint64_t)__double_as_longlong(x);
   const int E = (int)(ix >> 52);  // sign bit included: negative values fail the range test
+  if ((ix << 1) == 0) return x;   // sqrt(+-0) = +-0
   if (E == 0 || E >= 0x7ff) return sqrt(x);
   const uint64_t m = (ix & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   const int t = E - 1075;  // x = m 2^t
   const int odd = t & 1;
   // M = m 2^(52 + odd) in [2^104, 2^106); S = floor(sqrt(M)) in [2^52, 2^53)
   const uint64_t Z = m << (10 + odd);  // M / 2^42, in [2^62, 2^64)
-  // Y ~ 2^94 / sqrt(Z), in (2^62, 2^63]
-  const float zf = __ull2float_rz(Z >> 40);  // Z / 2^40
+  // Y ~ 2^94 / sqrt(Z), in (2^62, 2^63]: with g = Z / 2^62 = (m / 2^52) 2^odd
+  // in [1, 4) truncated to 24 bits, Y = rsqrt(g) 2^63 and rsqrt(g) in (1/2, 1]
+  const float g = __uint_as_float((uint32_t)((127 + odd) << 23) | (uint32_t)((m >> 29) & 0x7FFFFFu));
   float rs;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rs) : "f"(zf));
-  uint64_t Y = __float2ull_rz(rs * 0x1p74f);  // rs = 2^20 / sqrt(Z)
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rs) : "f"(g));
+  const uint32_t sb = __float_as_uint(rs);
+  uint64_t Y = (uint64_t)((sb & 0x7FFFFFu) | 0x800000u) << (39 + (int)(sb >> 23) - 126);
   for (int it = 0; it < 2; ++it) {
     // U = Z Y^2 / 2^128 ~ 2^60; Y <- Y (3 2^60 - U) / 2^61
     const uint64_t W = __umul64hi(Y, Y);
