@@ -99,9 +99,10 @@ def probe_fp64_peak(device=0):
 
 
 def selftest_arith(op, n, seed=1):
-    """Bit-for-bit check of the integer-pipe binary64 division (op 0) or
-    square root (op 1) against the hardware on n generated operand sets;
-    returns (mismatches, first mismatching {a, b, result})."""
+    """Bit-for-bit check of the integer-pipe binary64 routines against the
+    hardware on n generated operand sets: op 0 division, 1 square root,
+    2 comparisons, 3 fmax / fmin, 4 power-of-two scalings; returns
+    (mismatches, first mismatching {a, b, result})."""
     bad = C.c_uint64()
     ex = (C.c_double * 3)()
     rc = lib().fv2d_selftest_arith(int(op), int(n), int(seed), C.byref(bad), ex)

@@ -41,6 +41,41 @@ __host__ __device__ __forceinline__ double fv_sqrt(double x) {
 }
 __host__ __device__ __forceinline__ float fv_sqrt(float x) { return sqrtf(x); }
 
+// Comparisons, fmin / fmax and scalings by 1/2: on the device, binary64 goes
+// through the bit-pattern forms of softfp.cuh (IEEE results, integer pipe).
+#ifdef __CUDA_ARCH__
+#define FV2D_D(dev, host) return dev
+#else
+#define FV2D_D(dev, host) return host
+#endif
+__host__ __device__ __forceinline__ bool fv_gt0(double x) { FV2D_D(softfp::gt0(x), x > 0.0); }
+__host__ __device__ __forceinline__ bool fv_lt0(double x) { FV2D_D(softfp::lt0(x), x < 0.0); }
+__host__ __device__ __forceinline__ bool fv_ge0(double x) { FV2D_D(softfp::ge0(x), x >= 0.0); }
+__host__ __device__ __forceinline__ bool fv_le0(double x) { FV2D_D(softfp::le0(x), x <= 0.0); }
+__host__ __device__ __forceinline__ bool fv_lt(double x, double y) { FV2D_D(softfp::lt(x, y), x < y); }
+__host__ __device__ __forceinline__ bool fv_lt_abs(double x, double y) {
+  FV2D_D(softfp::lt_abs(x, y), fabs(x) < fabs(y));
+}
+__host__ __device__ __forceinline__ bool fv_prod_neg(double x, double y) {
+  FV2D_D(softfp::prod_neg(x, y), x * y < 0.0);
+}
+__host__ __device__ __forceinline__ double fv_fmax(double x, double y) { FV2D_D(softfp::fmax_nm(x, y), fmax(x, y)); }
+__host__ __device__ __forceinline__ double fv_fmin(double x, double y) { FV2D_D(softfp::fmin_nm(x, y), fmin(x, y)); }
+__host__ __device__ __forceinline__ double fv_half(double x) { FV2D_D(softfp::half(x), 0.5 * x); }
+__host__ __device__ __forceinline__ bool fv_isnan(double x) { FV2D_D(softfp::isnan_b(softfp::bits(x)), isnan(x)); }
+#undef FV2D_D
+__host__ __device__ __forceinline__ bool fv_gt0(float x) { return x > 0.0f; }
+__host__ __device__ __forceinline__ bool fv_lt0(float x) { return x < 0.0f; }
+__host__ __device__ __forceinline__ bool fv_ge0(float x) { return x >= 0.0f; }
+__host__ __device__ __forceinline__ bool fv_le0(float x) { return x <= 0.0f; }
+__host__ __device__ __forceinline__ bool fv_lt(float x, float y) { return x < y; }
+__host__ __device__ __forceinline__ bool fv_lt_abs(float x, float y) { return fabsf(x) < fabsf(y); }
+__host__ __device__ __forceinline__ bool fv_prod_neg(float x, float y) { return x * y < 0.0f; }
+__host__ __device__ __forceinline__ float fv_fmax(float x, float y) { return fmaxf(x, y); }
+__host__ __device__ __forceinline__ float fv_fmin(float x, float y) { return fminf(x, y); }
+__host__ __device__ __forceinline__ float fv_half(float x) { return 0.5f * x; }
+__host__ __device__ __forceinline__ bool fv_isnan(float x) { return isnan(x); }
+
 enum { IR = 0, IU = 1, IV = 2, IP = 3, IE = 3 };
 
 template <class R>
@@ -64,7 +99,7 @@ __host__ __device__ __forceinline__ S4<R> prim_to_cons(const S4<R> &q, const Gas
   s.r = q.r;
   s.u = q.r * q.u;
   s.v = q.r * q.v;
-  R Ek = fv_div(R(0.5) * (s.u * s.u + s.v * s.v), q.r);
+  R Ek = fv_div(fv_half(s.u * s.u + s.v * s.v), q.r);
   s.p = (Ek + fv_div(q.p, g.gm1));
   return s;
 }
@@ -76,7 +111,7 @@ __host__ __device__ __forceinline__ S4<R> cons_to_prim(const S4<R> &u, const Gas
   q.r = u.r;
   q.u = fv_div(u.u, u.r);
   q.v = fv_div(u.v, u.r);
-  R Ek = R(0.5) * q.r * (q.u * q.u + q.v * q.v);
+  R Ek = fv_half(q.r) * (q.u * q.u + q.v * q.v);
   q.p = (u.p - Ek) * g.gm1;
   return q;
 }
@@ -95,8 +130,8 @@ __device__ __forceinline__ R sound_speed(const S4<R> &q, const Gas<R> &g) {
 // Update.h:77-85
 template <class R>
 __host__ __device__ __forceinline__ R minmod(R dL, R dR) {
-  R m = (fabs(dL) < fabs(dR)) ? dL : dR;
-  return (dL * dR < R(0)) ? R(0) : m;
+  R m = fv_lt_abs(dL, dR) ? dL : dR;
+  return fv_prod_neg(dL, dR) ? R(0) : m;
 }
 
 template <class R>
@@ -114,14 +149,14 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   const R smaxL = qL.u + aL;
   const R sminR = qR.u - aR;
   const R smaxR = qR.u + aR;
-  const R SL = fmin(sminL, sminR);
-  const R SR = fmax(smaxL, smaxR);
+  const R SL = fv_fmin(sminL, sminR);
+  const R SR = fv_fmax(smaxL, smaxR);
   // computeFlux (RiemannSolvers.h:133-141).  p/(gamma-1) is also the pressure
   // term of primToCons below: the same division, evaluated once.
   const R peL = fv_div(qL.p, g.gm1);
   const R peR = fv_div(qR.p, g.gm1);
-  const R EkL = R(0.5) * qL.r * (qL.u * qL.u + qL.v * qL.v);
-  const R EkR = R(0.5) * qR.r * (qR.u * qR.u + qR.v * qR.v);
+  const R EkL = fv_half(qL.r) * (qL.u * qL.u + qL.v * qL.v);
+  const R EkR = fv_half(qR.r) * (qR.u * qR.u + qR.v * qR.v);
   const R EL = (peL + EkL);
   const R ER = (peR + EkR);
   const R ruL = qL.r * qL.u, ruR = qR.r * qR.u;
@@ -129,8 +164,8 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   S4<R> FR{ruR, ruR * qR.u + qR.p, ruR * qR.v, (qR.p + ER) * qR.u};
   // primToCons (States.h:19-30) of both states
   const R mvL = qL.r * qL.v, mvR = qR.r * qR.v;
-  const R uEL = (fv_div(R(0.5) * (ruL * ruL + mvL * mvL), qL.r) + peL);
-  const R uER = (fv_div(R(0.5) * (ruR * ruR + mvR * mvR), qR.r) + peR);
+  const R uEL = (fv_div(fv_half(ruL * ruL + mvL * mvL), qL.r) + peL);
+  const R uER = (fv_div(fv_half(ruR * ruR + mvR * mvR), qR.r) + peR);
   const R SLSR = SL * SR;
   const R den = SR - SL;
   S4<R> FM;
@@ -138,9 +173,9 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   FM.u = fv_div(SR * FL.u - SL * FR.u + SLSR * (ruR - ruL), den);
   FM.v = fv_div(SR * FL.v - SL * FR.v + SLSR * (mvR - mvL), den);
   FM.p = fv_div(SR * FL.p - SL * FR.p + SLSR * (uER - uEL), den);
-  const R pM = R(0.5) * (qL.p + qR.p);
-  const bool left = (SL >= R(0));
-  const bool right = !left && (SR <= R(0));
+  const R pM = fv_half(qL.p + qR.p);
+  const bool left = fv_ge0(SL);
+  const bool right = !left && fv_le0(SR);
   f.r = left ? FL.r : (right ? FR.r : FM.r);
   f.u = left ? FL.u : (right ? FR.u : FM.u);
   f.v = left ? FL.v : (right ? FR.v : FM.v);
@@ -155,20 +190,20 @@ template <class R>
 __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, const Gas<R> &g) {
   const R rL = qL.r, uL = qL.u, vL = qL.v, pL = qL.p;
   const R rR = qR.r, uR = qR.u, vR = qR.v, pR = qR.p;
-  const R ekL = R(0.5) * rL * (uL * uL + vL * vL);
+  const R ekL = fv_half(rL) * (uL * uL + vL * vL);
   const R EL = ekL + pL * g.entho;
-  const R ekR = R(0.5) * rR * (uR * uR + vR * vR);
+  const R ekR = fv_half(rR) * (uR * uR + vR * vR);
   const R ER = ekR + pR * g.entho;
   const R cL = sound_speed(qL, g);
   const R cR = sound_speed(qR, g);
-  const R cmax = fmax(cL, cR);
-  const R SL = fmin(uL, uR) - cmax;
-  const R SR = fmax(uL, uR) + cmax;
+  const R cmax = fv_fmax(cL, cR);
+  const R SL = fv_fmin(uL, uR) - cmax;
+  const R SR = fv_fmax(uL, uR) + cmax;
   const R rcL = rL * (uL - SL);
   const R rcR = rR * (SR - uR);
   const R uS = fv_div(rcR * uR + rcL * uL + (pL - pR), rcR + rcL);
   const R pS = fv_div(rcR * pL + rcL * pR + rcL * rcR * (uL - uR), rcR + rcL);
-  const bool sideL = (uS > R(0));
+  const bool sideL = fv_gt0(uS);
   const R rK = sideL ? rL : rR;
   const R uK = sideL ? uL : uR;
   const R pK = sideL ? pL : pR;
@@ -177,8 +212,8 @@ __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S
   const R rS = fv_div(rK * (SK - uK), SK - uS);
   const R ES = fv_div((SK - uK) * EK - pK * uK + pS * uS, SK - uS);
   // branch order of RiemannSolvers.h:89-112
-  const bool bL = (SL > R(0));
-  const bool bStar = !bL && (sideL || SR > R(0));
+  const bool bL = fv_gt0(SL);
+  const bool bStar = !bL && (sideL || fv_gt0(SR));
   R sr, su, sv, sp, E;
   if (bL) {
     sr = rL; su = uL; sv = vL; sp = pL; E = EL;
@@ -203,18 +238,18 @@ __device__ __forceinline__ void riemann_fslp(const S4<R> &qL, const S4<R> &qR, S
   const R rhoR = qR.r, uR = qR.u, pR = qR.p;
   const R csR = dsqrt(fv_div(g.gamma * pR, rhoR));
   const R zL = rhoL * csL, zR = rhoR * csR;
-  const R ai = g.fslp_K * ((zL < zR) ? zR : zL);
+  const R ai = g.fslp_K * (fv_lt(zL, zR) ? zR : zL);
   const R mL = fv_div(fabs(uL), csL), mR = fv_div(fabs(uR), csR);
-  const R mx = (mL < mR) ? mR : mL;
-  const R theta = (mx < R(1)) ? mx : R(1);
-  const R ustar = R(0.5) * (uR + uL) - fv_div(R(0.5), ai) * (pR - pL - R(0.5) * (rhoL + rhoR) * gdx);
-  const R Pi = R(0.5) * (pR + pL) - theta * R(0.5) * ai * (uR - uL);
-  const bool up = ustar > R(0);
+  const R mx = fv_lt(mL, mR) ? mR : mL;
+  const R theta = fv_lt(mx, R(1)) ? mx : R(1);
+  const R ustar = fv_half(uR + uL) - fv_div(R(0.5), ai) * (pR - pL - fv_half(rhoL + rhoR) * gdx);
+  const R Pi = fv_half(pR + pL) - fv_half(theta) * ai * (uR - uL);
+  const bool up = fv_gt0(ustar);
   const R sr = up ? qL.r : qR.r;
   const R su = up ? qL.u : qR.u;
   const R sv = up ? qL.v : qR.v;
   const R sp = up ? qL.p : qR.p;
-  const R Ekstar = R(0.5) * sr * (su * su + sv * sv);
+  const R Ekstar = fv_half(sr) * (su * su + sv * sv);
   const R Estar = Ekstar + fv_div(sp, g.gm1);
   f.r = ustar * sr;
   f.u = ustar * sr * su + Pi;

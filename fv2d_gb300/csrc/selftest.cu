@@ -1,5 +1,6 @@
-// selftest.cu -- checks the integer-pipe binary64 division and square root
-// (softfp.cuh) bit for bit against the hardware instructions on this GPU.
+// selftest.cu -- checks the integer-pipe binary64 routines of softfp.cuh bit
+// for bit against the hardware instructions on this GPU: op 0 division,
+// 1 square root, 2 comparisons, 3 fmax / fmin, 4 scalings by powers of two.
 #include <cuda_runtime.h>
 
 #include "../../include/fv2d_gpu.h"
@@ -57,16 +58,38 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
     }
     if (((r3 >> 20) & 15) == 0) a = copysign(0.0, a);  // zero dividends / radicands
     if (((r3 >> 24) & 63) == 0) b = copysign(0.0, b);  // division by zero
-    double h, s;
+    if (op >= 2 && ((r3 >> 30) & 3) == 0) b = a;  // equal operands
+    if (op >= 2 && ((r3 >> 44) & 7) == 0) b = -a;  // opposite operands (incl. +0 / -0)
+    namespace sf = fv2d::softfp;
+    double h, s, h2 = 0.0, s2 = 0.0;
     if (op == 0) {
       h = a / b;
-      s = fv2d::softfp::div_rn(a, b);
-    } else {
+      s = sf::div_rn(a, b);
+    } else if (op == 1) {
       a = fabs(a);
       h = sqrt(a);
-      s = fv2d::softfp::sqrt_rn(a);
+      s = sf::sqrt_rn(a);
+    } else if (op == 2) {  // comparisons, one bit each
+      h = (double)((a > 0.0) | (a < 0.0) << 1 | (a >= 0.0) << 2 | (a <= 0.0) << 3 | (a < b) << 4 |
+                   (fabs(a) < fabs(b)) << 5 | (a * b < 0.0) << 6 | (isnan(a) ? 1 : 0) << 7);
+      s = (double)(sf::gt0(a) | sf::lt0(a) << 1 | sf::ge0(a) << 2 | sf::le0(a) << 3 | sf::lt(a, b) << 4 |
+                   sf::lt_abs(a, b) << 5 | sf::prod_neg(a, b) << 6 | sf::isnan_b(sf::bits(a)) << 7);
+    } else if (op == 3) {  // fmax / fmin; +0 / -0 ties are ordered -0 < +0 by the bit forms
+      const bool zeros = a == 0.0 && b == 0.0;
+      h = zeros ? 0.0 : fmax(a, b);
+      s = zeros ? 0.0 : sf::fmax_nm(a, b);
+      h2 = zeros ? 0.0 : fmin(a, b);
+      s2 = zeros ? 0.0 : sf::fmin_nm(a, b);
+    } else {  // scalings by powers of two, including into and out of the subnormal range
+      const int k = (int)((r2 >> 40) % 121) - 60;
+      const double y = ldexp(1.0, k);
+      h = a * y;
+      s = sf::mul_pow2(a, y, k);
+      h2 = a * 0.5;
+      s2 = sf::half(a);
     }
-    const bool same = __double_as_longlong(h) == __double_as_longlong(s) || (h != h && s != s);
+    const bool same = (__double_as_longlong(h) == __double_as_longlong(s) || (h != h && s != s)) &&
+                      (__double_as_longlong(h2) == __double_as_longlong(s2) || (h2 != h2 && s2 != s2));
     if (!same) {
       const unsigned long long k = atomicAdd(bad, 1ull);
       if (k == 0) {
@@ -81,7 +104,7 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
 }  // namespace
 
 extern "C" int fv2d_selftest_arith(int op, uint64_t n, uint64_t seed, uint64_t *mismatches, double example[3]) {
-  if ((op != 0 && op != 1) || !mismatches) return FV2D_ERR_INVALID;
+  if (op < 0 || op > 4 || !mismatches) return FV2D_ERR_INVALID;
   unsigned long long *bad = nullptr;
   double *ex = nullptr;
   if (cudaMalloc(&bad, sizeof(*bad)) != cudaSuccess || cudaMalloc(&ex, 3 * sizeof(double)) != cudaSuccess) {

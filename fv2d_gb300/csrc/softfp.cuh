@@ -29,6 +29,20 @@
 namespace fv2d {
 namespace softfp {
 
+// The moves are opaque to the optimiser: a plain bit cast lets it recognise
+// the integer tests below as floating-point classifications and lower them
+// back to binary64 instructions (abs.f64 + setp).
+__device__ __forceinline__ uint64_t bits(double x) {
+  uint64_t b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+}
+__device__ __forceinline__ double from_bits(uint64_t b) {
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(b));
+  return x;
+}
+
 // The seeds are assembled from bit fields rather than by int64 <-> float
 // conversions, which issue on the binary64 pipe.
 __device__ __forceinline__ uint64_t recip_word(uint64_t d) {
@@ -72,7 +86,7 @@ __device__ __forceinline__ uint64_t recip_word(uint64_t d) {
 
 // a / b, round to nearest even.
 __device__ __forceinline__ double div_rn(double a, double b) {
-  const uint64_t ia = (uint64_t)__double_as_longlong(a), ib = (uint64_t)__double_as_longlong(b);
+  const uint64_t ia = bits(a), ib = bits(b);
   const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
   const uint64_t ma = (ia & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   const uint64_t mb = (ib & 0xFFFFFFFFFFFFFull) | (1ull << 52);
@@ -82,7 +96,7 @@ __device__ __forceinline__ double div_rn(double a, double b) {
     // +-0 / (finite nonzero normal) is a zero with the xor of the signs;
     // quiescent regions (zero momentum) make this the common special case.
     if ((ia << 1) == 0 && eb != 0 && eb != 0x7ff)
-      return __longlong_as_double((long long)((ia ^ ib) & 0x8000000000000000ull));
+      return from_bits((ia ^ ib) & 0x8000000000000000ull);
     return a / b;
   }
   // Q = floor(n 2^52 / mb) with n = ma or 2 ma, i.e. (n 2^63) / (mb 2^11)
@@ -109,13 +123,13 @@ __device__ __forceinline__ double div_rn(double a, double b) {
     Q >>= 1;
     ++e;
   }
-  const uint64_t bits = ((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull) | ((ia ^ ib) & 0x8000000000000000ull);
-  return __longlong_as_double((long long)bits);
+  const uint64_t out = ((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull) | ((ia ^ ib) & 0x8000000000000000ull);
+  return from_bits(out);
 }
 
 // sqrt(x), round to nearest even.
 __device__ __forceinline__ double sqrt_rn(double x) {
-  const uint64_t ix = (uint64_t)__double_as_longlong(x);
+  const uint64_t ix = bits(x);
   const int E = (int)(ix >> 52);  // sign bit included: negative values fail the range test
   if ((ix << 1) == 0) return x;   // sqrt(+-0) = +-0
   if (E == 0 || E >= 0x7ff) return sqrt(x);
@@ -158,8 +172,95 @@ __device__ __forceinline__ double sqrt_rn(double x) {
     Q >>= 1;
     ++e;
   }
-  return __longlong_as_double((long long)(((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull)));
+  return from_bits(((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull));
 }
+
+// ---------------------------------------------------------------------------
+// Comparisons and power-of-two scalings on the bit patterns.  Each returns
+// exactly what the IEEE operation returns (NaN compares false; +0 == -0),
+// so a binary64 DSETP / DMUL on the 1/64-rate pipe becomes a few integer
+// instructions.  Operands outside the cheap range (results that would be
+// subnormal, overflow, NaN/inf inputs of a product) go to the hardware
+// instruction through a call that is not if-converted.
+
+
+
+constexpr uint64_t MAG = 0x7FFFFFFFFFFFFFFFull, INF_BITS = 0x7FF0000000000000ull, SIGN = 0x8000000000000000ull;
+
+__device__ __forceinline__ bool isnan_b(uint64_t b) { return (b & MAG) > INF_BITS; }
+
+static __device__ __noinline__ double mul_hw(double x, double y) { return x * y; }
+static __device__ __noinline__ bool prod_neg_hw(double x, double y) { return x * y < 0.0; }
+
+// x > 0, x < 0, x >= 0, x <= 0
+__device__ __forceinline__ bool gt0(double x) { return bits(x) - 1ull < INF_BITS; }
+__device__ __forceinline__ bool lt0(double x) { return bits(x) - (SIGN + 1ull) < INF_BITS; }
+__device__ __forceinline__ bool ge0(double x) {
+  const uint64_t b = bits(x);
+  return b <= INF_BITS || b == SIGN;
+}
+__device__ __forceinline__ bool le0(double x) {
+  const uint64_t b = bits(x);
+  return (b & MAG) == 0 || b - SIGN <= INF_BITS;
+}
+
+// Order key with -0 == +0 (IEEE comparison order for non-NaN values).
+__device__ __forceinline__ int64_t key_ieee(uint64_t b) {
+  const int64_t m = (int64_t)(b & MAG);
+  return (int64_t)b < 0 ? -m : m;
+}
+// x < y (IEEE: false when either is NaN)
+__device__ __forceinline__ bool lt(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  return !isnan_b(a) && !isnan_b(b) && key_ieee(a) < key_ieee(b);
+}
+
+// maximumNumber / minimumNumber: a NaN operand yields the other one; -0 < +0.
+// (The C fmax / fmin of the aarch64 C library, FMAXNM / FMINNM.)
+__device__ __forceinline__ int64_t key_total(uint64_t b) { return (int64_t)(b ^ ((uint64_t)((int64_t)b >> 63) >> 1)); }
+__device__ __forceinline__ double fmax_nm(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  if (isnan_b(b)) return x;
+  if (isnan_b(a)) return y;
+  return key_total(a) > key_total(b) ? x : y;
+}
+__device__ __forceinline__ double fmin_nm(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  if (isnan_b(b)) return x;
+  if (isnan_b(a)) return y;
+  return key_total(a) < key_total(b) ? x : y;
+}
+
+// |x| < |y|
+__device__ __forceinline__ bool lt_abs(double x, double y) {
+  const uint64_t a = bits(x) & MAG, b = bits(y) & MAG;
+  return a < b && b <= INF_BITS;
+}
+
+// x * y < 0.  Nonzero non-NaN factors of opposite signs give a negative
+// product unless it underflows to -0, impossible when the biased exponents
+// sum to at least 972 (|x y| >= 2^-1074); smaller products go to hardware.
+__device__ __forceinline__ bool prod_neg(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  const uint64_t ma = a & MAG, mb = b & MAG;
+  if (!((a ^ b) & SIGN) || ma == 0 || mb == 0 || ma > INF_BITS || mb > INF_BITS) return false;
+  const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
+  if (ea != 0 && eb != 0 && ea + eb >= 972) return true;
+  return prod_neg_hw(x, y);
+}
+
+// x * 2^k for y == 2^k (k = unbiased exponent of y): exact exponent shift
+// when x and the result are normal; zeros keep their sign.
+__device__ __forceinline__ double mul_pow2(double x, double y, int k) {
+  const uint64_t a = bits(x);
+  const int e = (int)((a >> 52) & 0x7FF);
+  if ((a & MAG) == 0) return x;
+  if ((unsigned)(e - 1) < 0x7FEu && (unsigned)(e + k - 1) < 0x7FEu) return from_bits(a + ((uint64_t)(int64_t)k << 52));
+  return mul_hw(x, y);
+}
+
+// x * 0.5
+__device__ __forceinline__ double half(double x) { return mul_pow2(x, 0.5, -1); }
 
 }  // namespace softfp
 }  // namespace fv2d

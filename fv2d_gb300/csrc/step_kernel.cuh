@@ -78,7 +78,8 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err_flag) 
 __device__ __forceinline__ double ddivc(double x, double d, double inv_d, int pow2) {
   // x / d; when 1/d is exactly representable the product is the same
   // correctly rounded value.
-  return pow2 ? x * inv_d : fv_div(x, d);
+  if (pow2) return softfp::mul_pow2(x, inv_d, (int)((softfp::bits(inv_d) >> 52) & 0x7FF) - 1023);
+  return fv_div(x, d);
 }
 
 __device__ __forceinline__ double warp_max_nonneg(double v) {
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const double c = sQ(k, ly, lx);
-          sR1(L::SX, k, ly, lx) = minmod(c - sQ(k, ly, lx - 1), sQ(k, ly, lx + 1) - c) * 0.5;
+          sR1(L::SX, k, ly, lx) = fv_half(minmod(c - sQ(k, ly, lx - 1), sQ(k, ly, lx + 1) - c));
         }
       } else {
         const int jt = it - NXS;
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const double c = sQ(k, ly, lx);
-          sR1(L::SY, k, ly, lx) = minmod(c - sQ(k, ly - 1, lx), sQ(k, ly + 1, lx) - c) * 0.5;
+          sR1(L::SY, k, ly, lx) = fv_half(minmod(c - sQ(k, ly - 1, lx), sQ(k, ly + 1, lx) - c));
         }
       }
     }
@@ -417,14 +418,14 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
     // consToPrim (+ checkNegatives on the final stage)
     S4<double> q = cons_to_prim(S4<double>{un[0], un[1], un[2], un[3]}, gas);
     if (final_stage) {
-      if (q.r < 0) { q.r = a.eps_reset; ++cnt_rho; }
-      if (q.p < 0) { q.p = a.eps_reset; ++cnt_prs; }
-      cnt_nan += (unsigned)isnan(q.r) + (unsigned)isnan(q.u) + (unsigned)isnan(q.v) + (unsigned)isnan(q.p);
+      if (fv_lt0(q.r)) { q.r = a.eps_reset; ++cnt_rho; }
+      if (fv_lt0(q.p)) { q.p = a.eps_reset; ++cnt_prs; }
+      cnt_nan += (unsigned)fv_isnan(q.r) + (unsigned)fv_isnan(q.u) + (unsigned)fv_isnan(q.v) + (unsigned)fv_isnan(q.p);
       // inverse hyperbolic dt of the new state (ComputeDt.h:406-409)
       const double cs = sound_speed(q, gas);
       const double ih = ddivc(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2) +
                         ddivc(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2);
-      lmax = fmax(lmax, ih);
+      lmax = fv_fmax(lmax, ih);
     }
     Qd[g] = q.r;
     Qd[PL + g] = q.u;
