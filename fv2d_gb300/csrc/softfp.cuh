@@ -43,6 +43,12 @@ __device__ __forceinline__ double from_bits(uint64_t b) {
   return x;
 }
 
+// Hardware instructions for the special cases, behind calls so that the
+// compiler cannot if-convert their expansion into the common path (issued
+// predicated-off instructions still occupy the binary64 pipe).
+static __device__ __noinline__ double div_hw(double a, double b) { return a / b; }
+static __device__ __noinline__ double sqrt_hw(double x) { return sqrt(x); }
+
 // The seeds are assembled from bit fields rather than by int64 <-> float
 // conversions, which issue on the binary64 pipe.
 __device__ __forceinline__ uint64_t recip_word(uint64_t d) {
@@ -97,7 +103,7 @@ __device__ __forceinline__ double div_rn(double a, double b) {
     // quiescent regions (zero momentum) make this the common special case.
     if ((ia << 1) == 0 && eb != 0 && eb != 0x7ff)
       return from_bits((ia ^ ib) & 0x8000000000000000ull);
-    return a / b;
+    return div_hw(a, b);
   }
   // Q = floor(n 2^52 / mb) with n = ma or 2 ma, i.e. (n 2^63) / (mb 2^11)
   const uint64_t d = mb << 11;
@@ -132,7 +138,7 @@ __device__ __forceinline__ double sqrt_rn(double x) {
   const uint64_t ix = bits(x);
   const int E = (int)(ix >> 52);  // sign bit included: negative values fail the range test
   if ((ix << 1) == 0) return x;   // sqrt(+-0) = +-0
-  if (E == 0 || E >= 0x7ff) return sqrt(x);
+  if (E == 0 || E >= 0x7ff) return sqrt_hw(x);
   const uint64_t m = (ix & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   const int t = E - 1075;  // x = m 2^t
   const int odd = t & 1;

@@ -9,7 +9,7 @@
 namespace fv2d {
 
 // Tile of interior cells owned by one CTA of the fused step kernel.
-constexpr int TX = 32;  // cells along x (even: TMA rows start on 16-byte boundaries)
+constexpr int TX = 16;  // cells along x (even: TMA rows start on 16-byte boundaries)
 constexpr int TY = 16;  // cells along y
 constexpr int HALO = 2; // ghost depth read by PLM + the 3x3 viscous stencil
 constexpr int SW = TX + 2 * HALO;  // staged tile width  (TMA box x)

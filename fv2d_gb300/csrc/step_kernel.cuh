@@ -107,7 +107,7 @@ struct Smem {
 };
 
 template <int RECON, int RS>
-__global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
+__global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     step_kernel(const __grid_constant__ CUtensorMap tmQ0, const __grid_constant__ CUtensorMap tmQ1,
                 const StepArgs a) {
   using L = Smem<RECON>;
@@ -153,24 +153,44 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 2)
 
   // ---- 2. slopes (+ MUSCL-Hancock predictor) and temperatures ------------
   if constexpr (RECON == RECON_PLM) {
+    // Neighbour differences, once per face (the dR of one cell is the dL of
+    // the next: Update.h:70-76 computes both), held in the face-flux area
+    // until the Riemann pass: DX[k][r][f] = Q(f+1) - Q(f) on padded row r+2,
+    // DY[k][g][c] = Q(g+1) - Q(g) on padded column c+2.
+    constexpr int NDX = 4 * TY * (TX + 3), NDY = 4 * (TY + 3) * TX;
+    static_assert(NDX + NDY <= L::T - L::FX, "difference arrays exceed the face-flux area");
+    double *DX = sm + L::FX, *DY = sm + L::FX + NDX;
+    for (int it = tid; it < NDX + NDY; it += NT) {
+      if (it < NDX) {
+        const int k = it / (TY * (TX + 3)), rem = it % (TY * (TX + 3));
+        const int ly = rem / (TX + 3) + 2, lx = rem % (TX + 3) + 1;
+        DX[it] = sQ(k, ly, lx) - sQ(k, ly, lx - 1);
+      } else {
+        const int jt = it - NDX;
+        const int k = jt / ((TY + 3) * TX), rem = jt % ((TY + 3) * TX);
+        const int ly = rem / TX + 1, lx = rem % TX + 2;
+        DY[jt] = sQ(k, ly, lx) - sQ(k, ly - 1, lx);
+      }
+    }
+    __syncthreads();
     // half slopes 0.5*minmod: x at rows [2,TY+2) x cols [1,TX+3),
     // y at rows [1,TY+3) x cols [2,TX+2)
     constexpr int NXS = TY * (TX + 2), NYS = (TY + 2) * TX;
     for (int it = tid; it < NXS + NYS; it += NT) {
       if (it < NXS) {
-        const int ly = it / (TX + 2) + 2, lx = it % (TX + 2) + 1;
+        const int r = it / (TX + 2), c = it % (TX + 2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const double c = sQ(k, ly, lx);
-          sR1(L::SX, k, ly, lx) = fv_half(minmod(c - sQ(k, ly, lx - 1), sQ(k, ly, lx + 1) - c));
+          const double *d = DX + (k * TY + r) * (TX + 3) + c;  // d[0] = dL, d[1] = dR of column c+1
+          sR1(L::SX, k, r + 2, c + 1) = fv_half(minmod(d[0], d[1]));
         }
       } else {
         const int jt = it - NXS;
-        const int ly = jt / TX + 1, lx = jt % TX + 2;
+        const int g = jt / TX, c = jt % TX;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const double c = sQ(k, ly, lx);
-          sR1(L::SY, k, ly, lx) = fv_half(minmod(c - sQ(k, ly - 1, lx), sQ(k, ly + 1, lx) - c));
+          const double *d = DY + (k * (TY + 3) + g) * TX + c;  // d[0] = dU, d[TX] = dD of row g+1
+          sR1(L::SY, k, g + 1, c + 2) = fv_half(minmod(d[0], d[TX]));
         }
       }
     }
