@@ -101,7 +101,8 @@ def probe_fp64_peak(device=0):
 def selftest_arith(op, n, seed=1):
     """Bit-for-bit check of the integer-pipe binary64 routines against the
     hardware on n generated operand sets: op 0 division, 1 square root,
-    2 comparisons, 3 fmax / fmin, 4 power-of-two scalings; returns
+    2 comparisons, 3 fmax / fmin, 4 power-of-two scalings, 5 multiplication;
+    returns
     (mismatches, first mismatching {a, b, result})."""
     bad = C.c_uint64()
     ex = (C.c_double * 3)()

@@ -32,6 +32,19 @@ __host__ __device__ __forceinline__ double fv_div(double a, double b) {
 #endif
 }
 __host__ __device__ __forceinline__ float fv_div(float a, float b) { return a / b; }
+// a1 / b and a2 / b (one reciprocal of b on the device)
+__host__ __device__ __forceinline__ void fv_div2(double a1, double a2, double b, double &q1, double &q2) {
+#ifdef __CUDA_ARCH__
+  softfp::div2_rn(a1, a2, b, q1, q2);
+#else
+  q1 = a1 / b;
+  q2 = a2 / b;
+#endif
+}
+__host__ __device__ __forceinline__ void fv_div2(float a1, float a2, float b, float &q1, float &q2) {
+  q1 = a1 / b;
+  q2 = a2 / b;
+}
 __host__ __device__ __forceinline__ double fv_sqrt(double x) {
 #ifdef __CUDA_ARCH__
   return softfp::sqrt_rn(x);
@@ -62,6 +75,7 @@ __host__ __device__ __forceinline__ bool fv_prod_neg(double x, double y) {
 __host__ __device__ __forceinline__ double fv_fmax(double x, double y) { FV2D_D(softfp::fmax_nm(x, y), fmax(x, y)); }
 __host__ __device__ __forceinline__ double fv_fmin(double x, double y) { FV2D_D(softfp::fmin_nm(x, y), fmin(x, y)); }
 __host__ __device__ __forceinline__ double fv_half(double x) { FV2D_D(softfp::half(x), 0.5 * x); }
+__host__ __device__ __forceinline__ double fv_mul(double x, double y) { FV2D_D(softfp::mul_rn(x, y), x * y); }
 __host__ __device__ __forceinline__ bool fv_isnan(double x) { FV2D_D(softfp::isnan_b(softfp::bits(x)), isnan(x)); }
 #undef FV2D_D
 __host__ __device__ __forceinline__ bool fv_gt0(float x) { return x > 0.0f; }
@@ -74,7 +88,20 @@ __host__ __device__ __forceinline__ bool fv_prod_neg(float x, float y) { return 
 __host__ __device__ __forceinline__ float fv_fmax(float x, float y) { return fmaxf(x, y); }
 __host__ __device__ __forceinline__ float fv_fmin(float x, float y) { return fminf(x, y); }
 __host__ __device__ __forceinline__ float fv_half(float x) { return 0.5f * x; }
+__host__ __device__ __forceinline__ float fv_mul(float x, float y) { return x * y; }
 __host__ __device__ __forceinline__ bool fv_isnan(float x) { return isnan(x); }
+
+// Products moved from the binary64 pipe to the integer pipes (softfp::mul_rn),
+// by group: the step is bound by the binary64 pipe, and moving every product
+// would make the integer pipes the bound instead.
+#ifndef FV2D_SOFT_MUL
+#define FV2D_SOFT_MUL 1
+#endif
+template <int GROUP, class R>
+__host__ __device__ __forceinline__ R mulx(R a, R b) {
+  if constexpr (FV2D_SOFT_MUL >= GROUP) return fv_mul(a, b);
+  else return a * b;
+}
 
 enum { IR = 0, IU = 1, IV = 2, IP = 3, IE = 3 };
 
@@ -109,10 +136,9 @@ template <class R>
 __host__ __device__ __forceinline__ S4<R> cons_to_prim(const S4<R> &u, const Gas<R> &g) {
   S4<R> q;
   q.r = u.r;
-  q.u = fv_div(u.u, u.r);
-  q.v = fv_div(u.v, u.r);
-  R Ek = fv_half(q.r) * (q.u * q.u + q.v * q.v);
-  q.p = (u.p - Ek) * g.gm1;
+  fv_div2(u.u, u.v, u.r, q.u, q.v);
+  R Ek = mulx<3>(fv_half(q.r), mulx<3>(q.u, q.u) + mulx<3>(q.v, q.v));
+  q.p = mulx<3>(u.p - Ek, g.gm1);
   return q;
 }
 
@@ -124,7 +150,7 @@ __device__ __forceinline__ R dsqrt(R x) {
 // States.h:45-46
 template <class R>
 __device__ __forceinline__ R sound_speed(const S4<R> &q, const Gas<R> &g) {
-  return dsqrt(fv_div(q.p * g.gamma, q.r));
+  return dsqrt(fv_div(mulx<1>(q.p, g.gamma), q.r));
 }
 
 // Update.h:77-85
@@ -169,10 +195,10 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   const R SLSR = SL * SR;
   const R den = SR - SL;
   S4<R> FM;
-  FM.r = fv_div(SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r), den);
-  FM.u = fv_div(SR * FL.u - SL * FR.u + SLSR * (ruR - ruL), den);
-  FM.v = fv_div(SR * FL.v - SL * FR.v + SLSR * (mvR - mvL), den);
-  FM.p = fv_div(SR * FL.p - SL * FR.p + SLSR * (uER - uEL), den);
+  fv_div2(SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r), SR * FL.u - SL * FR.u + SLSR * (ruR - ruL), den, FM.r,
+          FM.u);
+  fv_div2(SR * FL.v - SL * FR.v + SLSR * (mvR - mvL), SR * FL.p - SL * FR.p + SLSR * (uER - uEL), den, FM.v,
+          FM.p);
   const R pM = fv_half(qL.p + qR.p);
   const bool left = fv_ge0(SL);
   const bool right = !left && fv_le0(SR);
@@ -190,27 +216,28 @@ template <class R>
 __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, const Gas<R> &g) {
   const R rL = qL.r, uL = qL.u, vL = qL.v, pL = qL.p;
   const R rR = qR.r, uR = qR.u, vR = qR.v, pR = qR.p;
-  const R ekL = fv_half(rL) * (uL * uL + vL * vL);
-  const R EL = ekL + pL * g.entho;
-  const R ekR = fv_half(rR) * (uR * uR + vR * vR);
-  const R ER = ekR + pR * g.entho;
+  const R ekL = mulx<2>(fv_half(rL), mulx<1>(uL, uL) + mulx<1>(vL, vL));
+  const R EL = ekL + mulx<1>(pL, g.entho);
+  const R ekR = mulx<2>(fv_half(rR), mulx<1>(uR, uR) + mulx<1>(vR, vR));
+  const R ER = ekR + mulx<1>(pR, g.entho);
   const R cL = sound_speed(qL, g);
   const R cR = sound_speed(qR, g);
   const R cmax = fv_fmax(cL, cR);
   const R SL = fv_fmin(uL, uR) - cmax;
   const R SR = fv_fmax(uL, uR) + cmax;
-  const R rcL = rL * (uL - SL);
-  const R rcR = rR * (SR - uR);
-  const R uS = fv_div(rcR * uR + rcL * uL + (pL - pR), rcR + rcL);
-  const R pS = fv_div(rcR * pL + rcL * pR + rcL * rcR * (uL - uR), rcR + rcL);
+  const R rcL = mulx<2>(rL, uL - SL);
+  const R rcR = mulx<2>(rR, SR - uR);
+  R uS, pS;
+  fv_div2(mulx<1>(rcR, uR) + mulx<1>(rcL, uL) + (pL - pR),
+          mulx<2>(rcR, pL) + mulx<2>(rcL, pR) + mulx<2>(mulx<2>(rcL, rcR), uL - uR), rcR + rcL, uS, pS);
   const bool sideL = fv_gt0(uS);
   const R rK = sideL ? rL : rR;
   const R uK = sideL ? uL : uR;
   const R pK = sideL ? pL : pR;
   const R EK = sideL ? EL : ER;
   const R SK = sideL ? SL : SR;
-  const R rS = fv_div(rK * (SK - uK), SK - uS);
-  const R ES = fv_div((SK - uK) * EK - pK * uK + pS * uS, SK - uS);
+  R rS, ES;
+  fv_div2(mulx<2>(rK, SK - uK), mulx<2>(SK - uK, EK) - mulx<2>(pK, uK) + mulx<2>(pS, uS), SK - uS, rS, ES);
   // branch order of RiemannSolvers.h:89-112
   const bool bL = fv_gt0(SL);
   const bool bStar = !bL && (sideL || fv_gt0(SR));
@@ -223,10 +250,10 @@ __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S
     sr = rR; su = uR; sv = vR; sp = pR; E = ER;
   }
   pout = sp;
-  f.r = sr * su;
-  f.u = sr * su * su + sp;
-  f.v = f.r * sv;
-  f.p = (E + sp) * su;
+  f.r = mulx<1>(sr, su);
+  f.u = mulx<1>(mulx<1>(sr, su), su) + sp;
+  f.v = mulx<1>(f.r, sv);
+  f.p = mulx<2>(E + sp, su);
 }
 
 // RiemannSolvers.h:130-171 (Kokkos::max / min as (a<b)?b:a and (b<a)?b:a).

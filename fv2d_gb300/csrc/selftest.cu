@@ -1,6 +1,7 @@
 // selftest.cu -- checks the integer-pipe binary64 routines of softfp.cuh bit
 // for bit against the hardware instructions on this GPU: op 0 division,
-// 1 square root, 2 comparisons, 3 fmax / fmin, 4 scalings by powers of two.
+// 1 square root, 2 comparisons, 3 fmax / fmin, 4 scalings by powers of two,
+// 5 multiplication.
 #include <cuda_runtime.h>
 
 #include "../../include/fv2d_gpu.h"
@@ -62,9 +63,14 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
     if (op >= 2 && ((r3 >> 44) & 7) == 0) b = -a;  // opposite operands (incl. +0 / -0)
     namespace sf = fv2d::softfp;
     double h, s, h2 = 0.0, s2 = 0.0;
-    if (op == 0) {
+    if (op == 0) {  // single quotient, and a pair sharing the divisor
       h = a / b;
       s = sf::div_rn(a, b);
+      const double c = ((r3 >> 56) & 3) == 0 ? 0.0 : operand(r2, r0, mode);
+      double s1;
+      sf::div2_rn(a, c, b, s1, s2);
+      h2 = c / b;
+      if (__double_as_longlong(s1) != __double_as_longlong(s) && !(s1 != s1 && s != s)) s2 = h2 + 1.0;
     } else if (op == 1) {
       a = fabs(a);
       h = sqrt(a);
@@ -80,6 +86,16 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
       s = zeros ? 0.0 : sf::fmax_nm(a, b);
       h2 = zeros ? 0.0 : fmin(a, b);
       s2 = zeros ? 0.0 : sf::fmin_nm(a, b);
+    } else if (op == 5) {  // products, including results next to the overflow and subnormal limits
+      if (((r3 >> 50) & 3) == 0) {
+        const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7FF);
+        const int target = ((r3 >> 52) & 1) ? (int)((r3 >> 53) % 7) - 3 : 2044 + (int)((r3 >> 53) % 7);
+        const int eb = target - ea + 1023;
+        if (eb >= 1 && eb <= 2046)
+          b = __longlong_as_double((long long)((r1 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)eb << 52)));
+      }
+      h = a * b;
+      s = sf::mul_rn(a, b);
     } else {  // scalings by powers of two, including into and out of the subnormal range
       const int k = (int)((r2 >> 40) % 121) - 60;
       const double y = ldexp(1.0, k);
@@ -104,7 +120,7 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
 }  // namespace
 
 extern "C" int fv2d_selftest_arith(int op, uint64_t n, uint64_t seed, uint64_t *mismatches, double example[3]) {
-  if (op < 0 || op > 4 || !mismatches) return FV2D_ERR_INVALID;
+  if (op < 0 || op > 5 || !mismatches) return FV2D_ERR_INVALID;
   unsigned long long *bad = nullptr;
   double *ex = nullptr;
   if (cudaMalloc(&bad, sizeof(*bad)) != cudaSuccess || cudaMalloc(&ex, 3 * sizeof(double)) != cudaSuccess) {

@@ -90,26 +90,43 @@ __device__ __forceinline__ uint64_t recip_word(uint64_t d) {
   return x;
 }
 
-// a / b, round to nearest even.
-__device__ __forceinline__ double div_rn(double a, double b) {
-  const uint64_t ia = bits(a), ib = bits(b);
-  const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
-  const uint64_t ma = (ia & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const uint64_t mb = (ib & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+// a / b, round to nearest even, in two halves so that quotients with a
+// common divisor share its reciprocal word: div_begin classifies the operands
+// and aligns the dividend, div_finish forms the quotient from v = recip_word(d)
+// (needed only when some quotient takes the fast path).
+struct DivOp {
+  uint64_t ia, ib, d, u1, u0;
+  int e;
+  bool fast;
+};
+
+__device__ __forceinline__ DivOp div_begin(double a, double b) {
+  DivOp o;
+  o.ia = bits(a);
+  o.ib = bits(b);
+  const int ea = (int)((o.ia >> 52) & 0x7ff), eb = (int)((o.ib >> 52) & 0x7ff);
+  const uint64_t ma = (o.ia & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const uint64_t mb = (o.ib & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   const bool big = ma >= mb;
-  int e = ea - eb + 1023 - (big ? 0 : 1);
-  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || e <= 0 || e >= 0x7fe) {
+  o.e = ea - eb + 1023 - (big ? 0 : 1);
+  o.fast = !(ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || o.e <= 0 || o.e >= 0x7fe);
+  // Q = floor(n 2^52 / mb) with n = ma or 2 ma, i.e. (n 2^63) / (mb 2^11)
+  o.d = mb << 11;
+  const uint64_t n = big ? ma : (ma << 1);
+  o.u1 = n >> 1;
+  o.u0 = n << 63;
+  return o;
+}
+
+__device__ __forceinline__ double div_finish(const DivOp &o, double a, double b, uint64_t v) {
+  if (!o.fast) {
     // +-0 / (finite nonzero normal) is a zero with the xor of the signs;
     // quiescent regions (zero momentum) make this the common special case.
-    if ((ia << 1) == 0 && eb != 0 && eb != 0x7ff)
-      return from_bits((ia ^ ib) & 0x8000000000000000ull);
+    const int eb = (int)((o.ib >> 52) & 0x7ff);
+    if ((o.ia << 1) == 0 && eb != 0 && eb != 0x7ff) return from_bits((o.ia ^ o.ib) & 0x8000000000000000ull);
     return div_hw(a, b);
   }
-  // Q = floor(n 2^52 / mb) with n = ma or 2 ma, i.e. (n 2^63) / (mb 2^11)
-  const uint64_t d = mb << 11;
-  const uint64_t n = big ? ma : (ma << 1);
-  const uint64_t u1 = n >> 1, u0 = n << 63;
-  const uint64_t v = recip_word(d);
+  const uint64_t d = o.d, u1 = o.u1, u0 = o.u0;
   uint64_t q0 = v * u1, q1 = __umul64hi(v, u1);
   const uint64_t s0 = q0 + u0;
   q1 = q1 + u1 + (s0 < q0) + 1;
@@ -125,12 +142,27 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   }
   // nearest even: compare 2 r with d
   uint64_t Q = q1 + ((r > d - r) || (r == d - r && (q1 & 1)));
+  int e = o.e;
   if (Q >> 53) {
     Q >>= 1;
     ++e;
   }
-  const uint64_t out = ((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull) | ((ia ^ ib) & 0x8000000000000000ull);
+  const uint64_t out = ((uint64_t)e << 52) | (Q & 0xFFFFFFFFFFFFFull) | ((o.ia ^ o.ib) & 0x8000000000000000ull);
   return from_bits(out);
+}
+
+__device__ __forceinline__ double div_rn(double a, double b) {
+  const DivOp o = div_begin(a, b);
+  const uint64_t v = o.fast ? recip_word(o.d) : 0ull;
+  return div_finish(o, a, b, v);
+}
+
+// a1 / b and a2 / b
+__device__ __forceinline__ void div2_rn(double a1, double a2, double b, double &q1, double &q2) {
+  const DivOp o1 = div_begin(a1, b), o2 = div_begin(a2, b);
+  const uint64_t v = (o1.fast || o2.fast) ? recip_word(o1.d) : 0ull;
+  q1 = div_finish(o1, a1, b, v);
+  q2 = div_finish(o2, a2, b, v);
 }
 
 // sqrt(x), round to nearest even.
@@ -267,6 +299,38 @@ __device__ __forceinline__ double mul_pow2(double x, double y, int k) {
 
 // x * 0.5
 __device__ __forceinline__ double half(double x) { return mul_pow2(x, 0.5, -1); }
+
+// x * y, round to nearest even, for normal operands with a normal result
+// (and zero times finite): the 106-bit product of the significands, cut at
+// bit 52 or 53 with the remainder deciding the rounding.  Subnormal, infinite
+// or NaN operands and results that overflow or fall below 2^-1022 (where the
+// subnormal grid changes the rounding) use the hardware instruction.
+__device__ __forceinline__ double mul_rn(double x, double y) {
+  const uint64_t a = bits(x), b = bits(y);
+  const uint64_t sgn = (a ^ b) & SIGN;
+  const int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);
+  if ((a & MAG) == 0 || (b & MAG) == 0) {
+    if (ea != 0x7FF && eb != 0x7FF) return from_bits(sgn);
+    return mul_hw(x, y);
+  }
+  int e = ea + eb - 1023;
+  if ((unsigned)(ea - 1) >= 0x7FEu || (unsigned)(eb - 1) >= 0x7FEu || (unsigned)(e - 1) >= 0x7FDu)
+    return mul_hw(x, y);
+  const uint64_t ma = (a & 0xFFFFFFFFFFFFFull) | (1ull << 52), mb = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const uint64_t lo = ma * mb, hi = __umul64hi(ma, mb);  // P = hi 2^64 + lo in [2^104, 2^106)
+  const int top = (int)(hi >> 41);                        // bit 105 of P
+  e += top;
+  const int s = 52 + top;
+  uint64_t M = (hi << (64 - s)) | (lo >> s);              // P >> s in [2^52, 2^53)
+  const uint64_t R = lo & ((1ull << s) - 1), H = 1ull << (s - 1);
+  M += (R > H) || (R == H && (M & 1));
+  if (M >> 53) {
+    M >>= 1;
+    ++e;
+  }
+  if (e >= 0x7FF) return mul_hw(x, y);
+  return from_bits(sgn | ((uint64_t)e << 52) | (M & 0xFFFFFFFFFFFFFull));
+}
 
 }  // namespace softfp
 }  // namespace fv2d

@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
       constexpr int S = TY * (TX + 1);
       const double FL0 = F[0], FR0 = F[1];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) un[k] += ddivc((F[k * S] - F[k * S + 1]) * dt, a.dx, a.inv_dx, a.dx_pow2);
+      for (int k = 0; k < 4; ++k) un[k] += ddivc(mulx<3>(F[k * S] - F[k * S + 1], dt), a.dx, a.inv_dx, a.dx_pow2);
       if (a.grav_mode) {
         const double gv = (a.grav_mode == 1) ? a.gxf : (double)a.grav_row[j];
         un[2] += dt * rho * gv;
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         }
       }
 #pragma unroll
-      for (int k = 0; k < 4; ++k) un[k] += ddivc((FL[k] - FR[k]) * dt, a.dy, a.inv_dy, a.dy_pow2);
+      for (int k = 0; k < 4; ++k) un[k] += ddivc(mulx<3>(FL[k] - FR[k], dt), a.dy, a.inv_dy, a.dy_pow2);
       if (a.grav_mode) {
         un[2] += dt * rho * gv;
         un[3] += dt * 0.5 * (FL[0] + FR[0]) * gv;

@@ -161,7 +161,7 @@ int fv2d_compute_dt_noalloc(const fv2d_params *p, const double *q_dev, double *o
 
 /* Self-test of the step kernel's binary64 arithmetic on the integer pipes:
  * op 0 = division, 1 = square root, 2 = comparisons, 3 = fmax / fmin,
- * 4 = scalings by powers of two.  Evaluates n generated operand sets
+ * 4 = scalings by powers of two, 5 = multiplication.  Evaluates n generated operand sets
  * (random significands, arbitrary bit patterns, near-tie and exact cases,
  * extreme exponents) with both the integer routine and the hardware
  * instruction and counts results whose bits differ (NaNs compare equal).

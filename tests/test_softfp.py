@@ -10,7 +10,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-NAMES = {0: "division", 1: "sqrt", 2: "comparisons", 3: "fmax/fmin", 4: "power-of-two scaling"}
+NAMES = {0: "division", 1: "sqrt", 2: "comparisons", 3: "fmax/fmin", 4: "power-of-two scaling", 5: "multiplication"}
 
 
 @pytest.mark.parametrize("op", sorted(NAMES))
