@@ -1,14 +1,14 @@
-// softfp.cuh -- correctly rounded binary64 division and square root computed
-// on the integer and FP32 pipes.
+// softfp.cuh -- binary64 arithmetic computed on the integer and FP32 pipes:
+// correctly rounded division, square root and multiplication, comparisons,
+// fmin / fmax and scalings by powers of two.
 //
 // GB300 executes binary64 at 1/64 of its FP32 rate; a hardware double
 // division or square root occupies that pipe for ~7-8 DFMA-equivalents while
 // the integer pipes stay idle in the FP64 step kernel.  These routines return
-// exactly the IEEE round-to-nearest-even result (the same bits as x / y and
-// sqrt(x)) for finite normal operands with a normal result and for zero
-// dividends and radicands, and defer every other case (subnormals,
-// infinities, NaNs, division by zero, overflow, underflow) to the hardware
-// instruction.
+// exactly the IEEE round-to-nearest-even result (the same bits as x / y,
+// sqrt(x), x * y) for finite normal operands with a normal result and for zero
+// operands, and defer every other case (subnormals, infinities, NaNs,
+// division by zero, overflow, underflow) to the hardware instruction.
 //
 // Division: the divisor's 53-bit significand is normalised to a 64-bit word d;
 // its reciprocal word v = floor((2^128 - 1) / d) - 2^64 (the definition of
