@@ -13,8 +13,10 @@ device from the previous state.
           with fv2d_run_async, timed with CUDA events on the library's stream
           (the state, 402 MB, is larger than the 129 MB L2, so no flush).
   e2e     the same metric through the C-ABI with host buffers: per step
-          fv2d_set_prim from page-locked host memory, fv2d_compute_dt,
-          fv2d_update, fv2d_get_prim into page-locked host memory.
+          fv2d_set_prim from page-locked host memory (read by the set-up
+          kernel over the host link), fv2d_compute_dt, fv2d_update (which
+          also writes the new state into a registered page-locked host
+          mirror while it computes), fv2d_get_prim on that mirror.
 
 `--impl reference` times the reference algorithm on the host cores: the
 CPU oracle (an OpenMP restatement of the reference's pass structure, bit-exact
@@ -382,6 +384,9 @@ def main():
     q1 = torch.empty_like(q0).pin_memory()
     sim.init_problem("sedov")
     sim.get_prim_ptr(q0.data_ptr())
+    # q1 is the context's host mirror: each fv2d_update writes the new state into
+    # it from the step kernel (over the host link, overlapped with the step)
+    sim.set_host_mirror(q1.data_ptr())
     ke = max(1, args.e2e_steps)
     for _ in range(2):
         sim.set_prim_ptr(q0.data_ptr())
@@ -401,7 +406,9 @@ def main():
         el_max = float(t.item())
     e2e = {"value": world * cells * ke / el_max, "unit": METRIC, "h2d_bytes_per_step": cells * 32,
            "d2h_bytes_per_step": cells * 32 + 8, "steps": ke,
-           "path": "fv2d_set_prim(pinned host) + fv2d_compute_dt + fv2d_update + fv2d_get_prim(pinned host)"}
+           "path": "fv2d_set_prim(pinned host, read by the set-up kernel) + fv2d_compute_dt + fv2d_update "
+                   "(writes the pinned host mirror while it computes) + fv2d_get_prim(mirror: waits for the step)"}
+    sim.set_host_mirror(0)
 
     extra = {}
     if not args.no_4096 and world == 1:

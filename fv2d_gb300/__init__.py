@@ -55,6 +55,7 @@ def lib():
         L.fv2d_get_cons.argtypes = [vp, _dp]
         L.fv2d_set_prim_device.argtypes = [vp, vp]
         L.fv2d_get_prim_device.argtypes = [vp, vp]
+        L.fv2d_set_host_mirror.argtypes = [vp, vp]
         L.fv2d_compute_dt.argtypes = [vp, _dp, _dp, _dp, _dp]
         L.fv2d_update.argtypes = [vp, C.c_double]
         L.fv2d_get_counters.argtypes = [vp, C.POINTER(C.c_uint64)]
@@ -179,6 +180,11 @@ class Simulation:
 
     def get_prim_ptr(self, host_ptr):
         self._check(self._lib.fv2d_get_prim(self.h, C.cast(C.c_void_p(host_ptr), _dp)))
+
+    def set_host_mirror(self, host_ptr):
+        """Register a page-locked (Ny, Nx, 4) float64 host array that every
+        update also writes the new primitives into (0 detaches)."""
+        self._check(self._lib.fv2d_set_host_mirror(self.h, C.c_void_p(host_ptr) if host_ptr else None))
 
     def set_prim_device(self, dev_ptr):
         self._check(self._lib.fv2d_set_prim_device(self.h, C.c_void_p(dev_ptr)))

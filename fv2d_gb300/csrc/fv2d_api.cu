@@ -51,6 +51,9 @@ struct fv2d_ctx {
   StepArgs args;
   double inv_tc = 0, inv_visc = 0;
   bool have_state = false;
+  double *mirror_host = nullptr;  // caller's page-locked array registered by fv2d_set_host_mirror
+  double *mirror_dev = nullptr;   // its device view
+  bool mirror_valid = false;      // it holds the current state (written by the last fv2d_update)
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   cudaStream_t graph_stream = nullptr;
@@ -286,6 +289,7 @@ int launch_update(fv2d_ctx *ctx, int driven, double dt) {
   StepArgs a = ctx->args;
   a.driven = driven;
   a.dt_arg = dt;
+  a.mirror = driven ? nullptr : ctx->mirror_dev;  // captured device loops never write it
   const dim3 grid((ctx->p.Nx + TX - 1) / TX, (ctx->p.Ny + TY - 1) / TY);
   const int rk = recon_kind(ctx->p.reconstruction);
   if (ctx->p.time_stepping == FV2D_TS_EULER) {
@@ -300,12 +304,25 @@ int launch_update(fv2d_ctx *ctx, int driven, double dt) {
   return FV2D_OK;
 }
 
-int run_prepare(fv2d_ctx *ctx) {
+// Device view of a page-locked (or registered) host array, or null when the
+// pointer is ordinary pageable memory.
+const double *mapped_host(const double *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<const double *>(at.devicePointer);
+}
+
+int run_prepare(fv2d_ctx *ctx, const double *src) {
   const fv2d_params &p = ctx->p;
   sync_state(ctx);  // reads the parity of the current buffer
+  ctx->mirror_valid = false;
   PrepArgs pa;
   std::memset(&pa, 0, sizeof(pa));
-  pa.q_aos = ctx->stage;
+  pa.q_aos = src;
   pa.Q = ctx->Q[ctx->st_host->parity];
   pa.U = ctx->U;
   pa.st = ctx->st;
@@ -511,14 +528,39 @@ int fv2d_set_prim_device(fv2d_ctx *ctx, const double *q_dev) {
   if (!ctx || !q_dev) return FV2D_ERR_INVALID;
   const size_t n = (size_t)ctx->p.Nx * ctx->p.Ny * 4;
   CK(cudaMemcpyAsync(ctx->stage, q_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  return run_prepare(ctx);
+  return run_prepare(ctx, ctx->stage);
 }
 
 int fv2d_set_prim(fv2d_ctx *ctx, const double *q_host) {
   if (!ctx || !q_host) return FV2D_ERR_INVALID;
-  const size_t n = (size_t)ctx->p.Nx * ctx->p.Ny * 4;
-  CK(cudaMemcpyAsync(ctx->stage, q_host, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  return run_prepare(ctx);
+  // Page-locked host memory is read by the set-up kernel itself over the
+  // host link (one pass instead of a copy then a pass); pageable memory is
+  // copied to the staging buffer first.
+  const double *src = mapped_host(q_host);
+  if (!src) {
+    const size_t n = (size_t)ctx->p.Nx * ctx->p.Ny * 4;
+    CK(cudaMemcpyAsync(ctx->stage, q_host, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    src = ctx->stage;
+  }
+  if (int rc = run_prepare(ctx, src)) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));  // q_host may be reused on return
+  return FV2D_OK;
+}
+
+int fv2d_set_host_mirror(fv2d_ctx *ctx, double *q_host) {
+  if (!ctx) return FV2D_ERR_INVALID;
+  CK(cudaStreamSynchronize(ctx->stream));  // no step in flight writes the old array
+  ctx->mirror_host = nullptr;
+  ctx->mirror_dev = nullptr;
+  ctx->mirror_valid = false;
+  if (!q_host) return FV2D_OK;
+  const double *dev = mapped_host(q_host);
+  if (!dev) return fail(ctx, FV2D_ERR_INVALID, "host mirror must be page-locked (cudaHostAlloc / cudaHostRegister)");
+  if ((reinterpret_cast<uintptr_t>(q_host) | reinterpret_cast<uintptr_t>(dev)) & 15)
+    return fail(ctx, FV2D_ERR_INVALID, "host mirror must be 16-byte aligned");
+  ctx->mirror_host = q_host;
+  ctx->mirror_dev = const_cast<double *>(dev);
+  return FV2D_OK;
 }
 
 int fv2d_init_problem(fv2d_ctx *ctx, int problem) {
@@ -529,7 +571,7 @@ int fv2d_init_problem(fv2d_ctx *ctx, int problem) {
   for (int j = 0; j < p.Ny; ++j)
     for (int i = 0; i < p.Nx; ++i) init_cell(p, problem, i, j, &q[((size_t)j * p.Nx + i) * 4]);
   CK(cudaMemcpyAsync(ctx->stage, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  int rc = run_prepare(ctx);
+  int rc = run_prepare(ctx, ctx->stage);
   if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));  // q is a local buffer
   return FV2D_OK;
@@ -550,6 +592,7 @@ int fv2d_get_prim(fv2d_ctx *ctx, double *q_host) {
   if (!ctx || !q_host) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   if (int rc = sync_state(ctx)) return rc;
+  if (ctx->mirror_valid && q_host == ctx->mirror_host) return FV2D_OK;  // the last update wrote it
   return get_planes(ctx, ctx->Q[ctx->st_host->parity], q_host, cudaMemcpyDeviceToHost);
 }
 
@@ -580,7 +623,10 @@ int fv2d_compute_dt(fv2d_ctx *ctx, double *dt, double *inv_hyp, double *inv_tc, 
 int fv2d_update(fv2d_ctx *ctx, double dt) {
   if (!ctx) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
-  return launch_update(ctx, 0, dt);
+  ctx->mirror_valid = false;
+  if (int rc = launch_update(ctx, 0, dt)) return rc;
+  ctx->mirror_valid = ctx->mirror_dev != nullptr;
+  return FV2D_OK;
 }
 
 int fv2d_get_counters(fv2d_ctx *ctx, uint64_t out[3]) {
@@ -613,6 +659,7 @@ int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, in
   if (!ctx) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   if (max_steps < 0) return fail(ctx, FV2D_ERR_INVALID, "max_steps < 0");
+  ctx->mirror_valid = false;
   const int check_save = next_save >= 0.0 ? 1 : 0;
   begin_kernel<<<1, 1, 0, ctx->stream>>>(ctx->st, tend, next_save, ctx->p.epsilon, check_save,
                                          skip_first_save_check, max_steps);
@@ -645,6 +692,7 @@ int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, in
 int fv2d_run_async(fv2d_ctx *ctx, int n) {
   if (!ctx || n < 0) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
+  ctx->mirror_valid = false;
   begin_kernel<<<1, 1, 0, ctx->stream>>>(ctx->st, INFINITY, -1.0, ctx->p.epsilon, 0, 1, n);
   CK(cudaGetLastError());
   if (int rc = ensure_graph(ctx)) return rc;

@@ -76,6 +76,8 @@ struct StepArgs {
   int grav_mode;  // 0 none, 1 constant, 2 analytical
   int tc, visc, wb;
   int bctc_ymin, bctc_ymax;
+  double *mirror;  // device view of a page-locked host (Ny x Nx x 4) array that the
+                   // final stage also writes the new primitives to (may be null)
 };
 
 // Set-up pass arguments (interior upload -> planes, ghosts, U, dt reduction).

@@ -451,6 +451,11 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     Qd[PL + g] = q.u;
     Qd[2 * PL + g] = q.v;
     Qd[3 * PL + g] = q.p;
+    if (final_stage && a.mirror) {  // interleaved interior copy in host memory (over the C2C link)
+      double2 *m = reinterpret_cast<double2 *>(a.mirror + ((long long)j * a.Nx + i) * 4);
+      m[0] = make_double2(q.r, q.u);
+      m[1] = make_double2(q.v, q.p);
+    }
     // ghost cells that copy this cell (BoundaryConditions.h:82-147)
     const bool ex = (i < 2 || i >= a.Nx - 2), ey = (j < 2 || j >= a.Ny - 2);
     if (ex || ey) {

@@ -65,10 +65,20 @@ int fv2d_set_stream(fv2d_ctx *ctx, void *stream);
 int fv2d_init_problem(fv2d_ctx *ctx, int problem);
 
 /* Interior primitive state (Ny x Nx x {rho,u,v,p}) from / to host memory.
- * set_prim behaves like a restart: boundary fill, primToCons, dt reduction.
- * Page-locked host memory gives full copy bandwidth. */
+ * set_prim behaves like a restart: boundary fill, primToCons, dt reduction;
+ * it returns once q_host has been consumed.  Page-locked host memory is read
+ * by the set-up kernel directly over the host link (no staging copy). */
 int fv2d_set_prim(fv2d_ctx *ctx, const double *q_host);
 int fv2d_get_prim(fv2d_ctx *ctx, double *q_host);
+
+/* Host mirror (no reference counterpart): registers a page-locked, 16-byte
+ * aligned host array of Ny x Nx x 4 doubles that every fv2d_update also
+ * writes the new interior primitives into, from the step kernel itself while
+ * it computes (the transfer overlaps the step instead of following it).
+ * fv2d_get_prim on that same pointer then only waits for the step.  The
+ * device-driven loops (fv2d_advance, fv2d_run_async) do not write it.  NULL
+ * detaches; the array must stay valid while registered. */
+int fv2d_set_host_mirror(fv2d_ctx *ctx, double *q_host);
 /* Interior conservative state (rho, rho u, rho v, E). */
 int fv2d_get_cons(fv2d_ctx *ctx, double *u_host);
 
