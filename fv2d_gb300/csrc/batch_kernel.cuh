@@ -59,8 +59,10 @@ template <int TX, int TY, int NT, int STAGING>
 __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
   using L = BatchSmem<TX, TY>;
   constexpr int SW = L::SW, SH = L::SH;
-  extern __shared__ unsigned char smem_raw[];
-  float *sm = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // Aligned by offsetting the shared array itself (not through an integer
+  // round trip, which would turn every tile access into a generic load).
+  extern __shared__ __align__(128) unsigned char fv2d_batch_smem[];
+  float *sm = reinterpret_cast<float *>(fv2d_batch_smem + ((128u - ((uint32_t)__cvta_generic_to_shared(fv2d_batch_smem) & 127u)) & 127u));
   __shared__ SimDev S;
   __shared__ __align__(8) uint64_t mbar;
   __shared__ float red_max[NT / 32];

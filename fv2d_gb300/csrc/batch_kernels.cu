@@ -3,6 +3,7 @@
 // Compiled with fast single-precision math: the service's tolerance is set
 // against the binary64 path, not bit parity.
 #include "batch_kernel.cuh"
+#include "batch_march.cuh"
 
 namespace fv2d {
 
@@ -16,6 +17,12 @@ struct BatchCfg {
 #define FV2D_CFG(TX, TY, NT, ST, NAME) \
   {TX, TY, NT, ST, NAME, BatchSmem<TX, TY>::BYTES, (const void *)batch_step_kernel<TX, TY, NT, ST>}
 
+// Column-marching configurations (batch_march.cuh): 28 interior columns per
+// warp, H rows per work item, no shared memory (staging code 2).
+// MINB caps the registers so that MINB CTAs fit on an SM.
+#define FV2D_MARCH(H, NT, MINB, NAME) \
+  {bm::STRIP, H, NT, 2, NAME, 0, (const void *)batch_march_kernel<H, NT, MINB>}
+
 static const BatchCfg kCfgs[] = {
     FV2D_CFG(32, 8, 128, 0, "32x8/128/ldg"),
     FV2D_CFG(32, 16, 256, 0, "32x16/256/ldg"),
@@ -23,6 +30,10 @@ static const BatchCfg kCfgs[] = {
     FV2D_CFG(32, 32, 256, 1, "32x32/256/tma"),
     FV2D_CFG(32, 32, 512, 0, "32x32/512/ldg"),
     FV2D_CFG(64, 16, 256, 1, "64x16/256/tma"),
+    FV2D_MARCH(32, 128, 4, "28x32/128/march"),
+    FV2D_MARCH(64, 128, 4, "28x64/128/march"),
+    FV2D_MARCH(32, 128, 5, "28x32/128x5/march"),
+    FV2D_MARCH(64, 128, 5, "28x64/128x5/march"),
 };
 
 int batch_num_cfgs() { return (int)(sizeof(kCfgs) / sizeof(kCfgs[0])); }

@@ -401,7 +401,7 @@ int admit(fv2d_server *s, const Pending &pd) {
   d.visc = p.viscosity_active ? 1 : 0;
   d.lowmach = r.lowmach ? 1 : 0;
   d.tma_ok = 0;
-  if (staging) {
+  if (staging == 1) {  // TMA staging needs the tensor maps
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     bool ok = enc != nullptr;
     for (int b = 0; b < 2 && ok; ++b) {
@@ -811,7 +811,11 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
     int per_sm = 0;
     if (batch_setup(c, &per_sm) == cudaSuccess && per_sm > 0) s->cfg_grid[c] = per_sm * s->num_sms;
   }
-  if (cfg->autotune) autotune(s);
+  if (cfg->tile_config > 0 && cfg->tile_config <= batch_num_cfgs() && s->cfg_grid[cfg->tile_config - 1]) {
+    for (int b = 0; b < kBuckets; ++b) s->bucket_cfg[b] = cfg->tile_config - 1;
+  } else if (cfg->autotune) {
+    autotune(s);
+  }
   s->worker = std::thread(worker_main, s);
   *out = s;
   return FV2D_OK;

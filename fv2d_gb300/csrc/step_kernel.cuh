@@ -111,8 +111,10 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     step_kernel(const __grid_constant__ CUtensorMap tmQ0, const __grid_constant__ CUtensorMap tmQ1,
                 const StepArgs a) {
   using L = Smem<RECON>;
-  extern __shared__ unsigned char smem_raw[];
-  double *sm = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // Aligned by offsetting the shared array itself (not through an integer
+  // round trip, which would turn every tile access into a generic load).
+  extern __shared__ __align__(128) unsigned char fv2d_step_smem[];
+  double *sm = reinterpret_cast<double *>(fv2d_step_smem + ((128u - ((uint32_t)__cvta_generic_to_shared(fv2d_step_smem) & 127u)) & 127u));
   __shared__ __align__(8) uint64_t mbar;
   __shared__ double red_max[NT / 32];
   __shared__ unsigned red_cnt[3][NT / 32];

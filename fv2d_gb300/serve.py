@@ -12,7 +12,7 @@ from ._abi import Params, PROBLEMS, as_float32
 class ServerConfig(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("device", C.c_int32), ("budget_bytes", C.c_double),
                 ("max_sims", C.c_int32), ("autotune", C.c_int32), ("steps_per_replay", C.c_int32),
-                ("pad", C.c_int32)]
+                ("tile_config", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -64,13 +64,32 @@ def config_name(index):
     return v.decode() if v else None
 
 
+def config_names():
+    """Names of the kernel configurations, by index."""
+    out = []
+    while True:
+        n = config_name(len(out))
+        if n is None:
+            return out
+        out.append(n)
+
+
 class Server:
     """A running batched service on one GPU."""
 
-    def __init__(self, budget_bytes=150e9, device=0, max_sims=4096, autotune=True, steps_per_replay=0):
+    def __init__(self, budget_bytes=150e9, device=0, max_sims=4096, autotune=True, steps_per_replay=0,
+                 tile_config=None):
+        """tile_config: name of a kernel configuration (config_name) to use for
+        every grid-size bucket instead of the defaults or the autotuner."""
         self.L = _bind(_lib_loader())
+        forced = 0
+        if tile_config is not None:
+            names = config_names()
+            if tile_config not in names:
+                raise ValueError(f"unknown tile configuration {tile_config!r}; known: {names}")
+            forced = names.index(tile_config) + 1
         cfg = ServerConfig(C.sizeof(ServerConfig), device, float(budget_bytes), max_sims, 1 if autotune else 0,
-                           steps_per_replay, 0)
+                           steps_per_replay, forced)
         self.h = C.c_void_p()
         rc = self.L.fv2d_server_create(C.byref(cfg), C.byref(self.h))
         if rc != 0:

@@ -41,7 +41,7 @@ typedef struct fv2d_server_config {
   int32_t max_sims;         /* simulation table capacity (<= 16384) */
   int32_t autotune;         /* 1: time the tile configurations per bucket at start-up */
   int32_t steps_per_replay; /* 0: adaptive (about 3 ms of work per graph replay) */
-  int32_t pad;
+  int32_t tile_config;      /* 0: defaults or autotuned; k > 0: configuration k - 1 for every bucket */
 } fv2d_server_config;
 
 typedef struct fv2d_request {

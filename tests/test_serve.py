@@ -38,18 +38,23 @@ def mixed_requests():
     ]
 
 
-def test_same_result_alone_and_in_the_mix(gpu_lib):
+# the default tile kernel and the register-resident column-marching kernel
+TILES = [None, "28x64/128/march"]
+
+
+@pytest.mark.parametrize("tile", TILES)
+def test_same_result_alone_and_in_the_mix(gpu_lib, tile):
     from fv2d_gb300.serve import Server
     reqs = mixed_requests()
     alone = []
-    with Server(budget_bytes=4e9, autotune=False) as s:
+    with Server(budget_bytes=4e9, autotune=False, tile_config=tile) as s:
         for pb, p, n, lm in reqs:
             rid = s.submit(pb, p, n, lowmach=lm)
             assert s.drain(120) == 0
             res = {r.id: r for r in s.poll()}
             assert res[rid].status == 0 and res[rid].steps == n
             alone.append((s.get_prim(rid), res[rid].t))
-    with Server(budget_bytes=4e9, autotune=False) as s:
+    with Server(budget_bytes=4e9, autotune=False, tile_config=tile) as s:
         fillers = [s.submit("sedov", params(N), 30 + N // 16) for N in (64, 320, 512, 192, 96)]
         ids = [s.submit(pb, p, n, lowmach=lm) for pb, p, n, lm in reqs]
         fillers += [s.submit("kh_step", params(N, boundary_x=2, boundary_y=2), 45) for N in (128, 224)]
@@ -66,7 +71,8 @@ def l1_rel(a, b):
     return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
 
 
-def test_accuracy_against_fp64_path(gpu_lib):
+@pytest.mark.parametrize("tile", TILES)
+def test_accuracy_against_fp64_path(gpu_lib, tile):
     """Each request against the binary64 plain path from the same initial
     condition after the same number of steps."""
     import fv2d_gb300 as fv
@@ -79,7 +85,7 @@ def test_accuracy_against_fp64_path(gpu_lib):
                                  gresho_Mach=fv.as_float32(0.1)), 200, True),
     ]
     report = {}
-    with Server(budget_bytes=4e9, autotune=False) as s:
+    with Server(budget_bytes=4e9, autotune=False, tile_config=tile) as s:
         ids = [s.submit(pb, p, n, lowmach=lm) for pb, p, n, lm in cases]
         assert s.drain(120) == 0
         res = {r.id: r for r in s.poll()}
