@@ -253,3 +253,39 @@ def test_page_locked_input_and_host_mirror_match_pageable_path(gpu_lib):
         a.set_host_mirror(0)
         a.close()
         b.close()
+
+
+def test_page_locked_rounds_match_oracle(gpu_lib):
+    """Rounds of set_prim from page-locked memory (read by the set-up kernel),
+    compute_dt, update writing the host mirror and get_prim on the mirror --
+    the end-to-end benchmark's call sequence -- give the oracle's bits for
+    every Euler combination of PCM / PCM_WB / PLM, HLL / HLLC, boundaries
+    and gravity, on a grid that cuts tiles."""
+    torch = pytest.importorskip("torch")
+    ny, nx = 37, 50
+    q0 = random_prim(ny, nx, 9)
+    pin_in = torch.from_numpy(q0.copy()).pin_memory()
+    pin_out = torch.zeros((ny, nx, 4), dtype=torch.float64).pin_memory()
+    combos = [c for c in G.combo_list() if c.get("time_stepping", 0) == 0 and c.get("riemann_solver", 1) in (0, 1)
+              and not c.get("thermal_conductivity_active") and not c.get("viscosity_active")
+              and not c.get("well_balanced_flux_at_y_bc")]
+    assert len(combos) >= 18
+    for c in combos:
+        p = reference_params(Nx=nx, Ny=ny, gamma0=1.4, CFL=0.6, **c)
+        s, o = gpu_sim(p), Oracle(p)
+        s.set_host_mirror(pin_out.data_ptr())
+        q = q0
+        for _ in range(3):
+            pin_in.numpy()[...] = q
+            s.set_prim_ptr(pin_in.data_ptr())
+            o.set_prim(q)
+            d = o.compute_dt()
+            assert bits_equal(s.compute_dt()[0], d[0]), c
+            s.update(d[0])
+            o.update(d[0])
+            s.get_prim_ptr(pin_out.data_ptr())
+            q = o.get_prim()
+            assert bits_equal(pin_out.numpy(), q), c
+            assert bits_equal(s.get_cons(), o.get_cons()), c
+        s.set_host_mirror(0)
+        s.close()
