@@ -33,13 +33,27 @@ struct __align__(64) SimDev {
   int recon;            // 0 PCM, 2 PLM
   int bcx, bcy;
   int grav, tc, visc;
-  int lowmach;          // recover p = (E - Ek)(gamma - 1) in binary64
+  int lowmach;          // recover p = (E - Ek)(gamma - 1) in binary64 where it cancels
   unsigned int acc_bits;  // running max of the inverse hyperbolic dt (float bits)
   unsigned int ticket;    // tiles finished in the running launch
   unsigned long long negatives;  // cells reset by the negative guard (all steps)
   int tma_ok;           // tensor map valid for this simulation
   int pad0;
 };
+
+// Pressure (E - rho |u|^2 / 2)(gamma - 1) of the binary32 state.  Low-Mach
+// requests recover it in binary64 where it cancels: when the kinetic energy is
+// more than a quarter of E the subtraction loses two or more bits.  Elsewhere
+// the binary32 evaluation is within a unit or two of the binary64 one rounded
+// to binary32, so the binary64 pipe (1/64 of the FP32 rate) is not used.
+__device__ __forceinline__ float pressure_of(float E, float r, float u, float v, float gm1, int lowmach) {
+  const float ek = 0.5f * r * (u * u + v * v);
+  if (lowmach && fabsf(ek) > 0.25f * fabsf(E)) {
+    const double rd = r, ud = u, vd = v;
+    return (float)(((double)E - 0.5 * rd * (ud * ud + vd * vd)) * (double)gm1);
+  }
+  return (E - ek) * gm1;
+}
 
 // A tile of one simulation: sim index in the table, tile coordinates.
 struct WorkItem {

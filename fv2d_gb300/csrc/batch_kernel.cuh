@@ -6,7 +6,8 @@
 //     state) into shared memory, by one TMA load from the simulation's tensor
 //     map or by cooperative 16-byte loads (STAGING, picked by the autotuner);
 //   - consToPrim with the negative reset (States.h:32-43, SimInfo.h:618-627);
-//     low-Mach simulations recover p = (E - Ek)(gamma - 1) in binary64;
+//     low-Mach simulations recover p = (E - Ek)(gamma - 1) in binary64
+//     where it cancels (pressure_of);
 //   - minmod half slopes, one Riemann solve per face (HLL or HLLC), update
 //     in the reference's order (x flux, x gravity, y flux, y gravity,
 //     conduction, viscosity) in binary32 with fused multiply-adds;
@@ -139,13 +140,8 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
     for (int e = tid; e < SH * SW; e += NT) {
       const int ly = e / SW, lx = e % SW;
       float r = sQ(0, ly, lx), mu = sQ(1, ly, lx), mv = sQ(2, ly, lx), E = sQ(3, ly, lx);
-      float u = mu / r, v = mv / r, p;
-      if (S.lowmach) {
-        const double rd = r, ud = u, vd = v;
-        p = (float)(((double)E - 0.5 * rd * (ud * ud + vd * vd)) * (double)S.gm1);
-      } else {
-        p = (E - 0.5f * r * (u * u + v * v)) * S.gm1;
-      }
+      float u = mu / r, v = mv / r;
+      float p = pressure_of(E, r, u, v, S.gm1, S.lowmach);
       if (r < 0.f) r = 1e-8f;
       if (p < 0.f) p = 1e-8f;
       sQ(0, ly, lx) = r;
@@ -305,9 +301,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
       for (int k = 0; k < 4; ++k) dst[k * PL + g] = un[k];
       // primitive state of the new cell for the next dt
       float r = un[0], u = un[1] / r, v = un[2] / r;
-      float p = (un[3] - 0.5f * r * (u * u + v * v)) * S.gm1;
-      if (S.lowmach)
-        p = (float)(((double)un[3] - 0.5 * (double)r * ((double)u * u + (double)v * v)) * (double)S.gm1);
+      float p = pressure_of(un[3], r, u, v, S.gm1, S.lowmach);
       nneg += (r < 0.f) + (p < 0.f);
       if (r < 0.f) r = 1e-8f;
       if (p < 0.f) p = 1e-8f;

@@ -55,13 +55,7 @@ struct SimView {
 __device__ __forceinline__ S4<float> to_prim(const float u[4], const SimView &S) {
   float r = u[0];
   const float uu = u[1] / r, vv = u[2] / r;
-  float p;
-  if (S.lowmach) {
-    const double rd = r, ud = uu, vd = vv;
-    p = (float)(((double)u[3] - 0.5 * rd * (ud * ud + vd * vd)) * (double)S.gm1);
-  } else {
-    p = (u[3] - 0.5f * r * (uu * uu + vv * vv)) * S.gm1;
-  }
+  float p = pressure_of(u[3], r, uu, vv, S.gm1, S.lowmach);
   if (r < 0.f) r = 1e-8f;
   if (p < 0.f) p = 1e-8f;
   return S4<float>{r, uu, vv, p};
@@ -258,9 +252,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a
         for (int k = 0; k < 4; ++k) S.dst[k * S.PL + g] = un[k];
         // primitive state of the new cell for the next dt
         float r = un[0], u = un[1] / r, v = un[2] / r;
-        float p = (un[3] - 0.5f * r * (u * u + v * v)) * S.gm1;
-        if (S.lowmach)
-          p = (float)(((double)un[3] - 0.5 * (double)r * ((double)u * u + (double)v * v)) * (double)S.gm1);
+        float p = pressure_of(un[3], r, u, v, S.gm1, S.lowmach);
         nneg += (r < 0.f) + (p < 0.f);
         if (r < 0.f) r = 1e-8f;
         if (p < 0.f) p = 1e-8f;

@@ -88,9 +88,7 @@ __global__ void first_dt_kernel(SimDev *sims, int slot) {
     const int j = (int)(c / N), i = (int)(c % N);
     const long long g = (long long)(j + 2) * S.pitch + (i + 2);
     float r = U[g], u = U[S.plane + g] / r, v = U[2 * S.plane + g] / r;
-    float p = (U[3 * S.plane + g] - 0.5f * r * (u * u + v * v)) * S.gm1;
-    if (S.lowmach)
-      p = (float)(((double)U[3 * S.plane + g] - 0.5 * (double)r * ((double)u * u + (double)v * v)) * (double)S.gm1);
+    float p = pressure_of(U[3 * S.plane + g], r, u, v, S.gm1, S.lowmach);
     if (r < 0.f) r = 1e-8f;
     if (p < 0.f) p = 1e-8f;
     const float cs = sqrtf(p * S.gamma / r);

@@ -50,7 +50,7 @@ typedef struct fv2d_request {
   fv2d_params params;/* Nx == Ny == N (multiple of 32, 64..4096); PCM or PLM; HLL or HLLC; Euler;
                         constant gravity, constant conductivity and viscosity allowed */
   int32_t max_steps; /* stop after this many steps */
-  int32_t lowmach;   /* 1: recover the pressure from E - rho|u|^2/2 in binary64 */
+  int32_t lowmach;   /* 1: recover the pressure from E - rho|u|^2/2 in binary64 where it cancels */
   double tend;       /* also stop once t + epsilon >= tend (<= 0: no time limit) */
 } fv2d_request;
 
