@@ -279,6 +279,10 @@ def main():
     ap.add_argument("--served-only", action="store_true", help="only the batched FP32 service on the stream")
     ap.add_argument("--served-profile", action="store_true",
                     help="fixed batch for kernel profiling: 12 Sedov 768^2 requests x 60 steps")
+    ap.add_argument("--served-saturated", action="store_true",
+                    help="service rate without arrival gaps: the request stream submitted at once")
+    ap.add_argument("--served-tile", default=None,
+                    help="kernel configuration for every bucket of the profiling batch (e.g. 28x64/128/march)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -292,9 +296,32 @@ def main():
     if not os.path.exists(fv.LIB_PATH):
         from fv2d_gb300 import build as b
         b.build()
+    if args.served_saturated:
+        from fv2d_gb300.serve import Server, stream_requests, config_name
+        reqs = stream_requests(n=args.served_requests)
+        with Server(budget_bytes=150e9, device=local, autotune=args.served_tile is None,
+                    tile_config=args.served_tile) as srv:
+            t0 = time.perf_counter()
+            for r in reqs:
+                srv.submit(r["problem"], r["params"], r["steps"], lowmach=r["lowmach"])
+            lat = []
+            while len(lat) < len(reqs):
+                for x in srv.poll():
+                    lat.append(x.done_s - x.submit_s)
+                    srv.release(x.id)
+                time.sleep(0.0005)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+            work = sum(float(r["N"]) ** 2 * r["steps"] for r in reqs)
+            print(json.dumps({"served_saturated": True, "requests": len(reqs), "cell_updates": work,
+                              "wall_s": wall, "rate": work / wall, "unit": METRIC,
+                              "p50_s": float(np.median(lat)), "p99_s": float(np.percentile(lat, 99)),
+                              "tile_configs_per_bucket": [config_name(st.bucket_cfg[b]) for b in range(4)]}),
+                  flush=True)
+        return
     if args.served_profile:
         from fv2d_gb300.serve import Server
-        with Server(budget_bytes=20e9, device=local, autotune=False) as srv:
+        with Server(budget_bytes=20e9, device=local, autotune=False, tile_config=args.served_tile) as srv:
             p = workload_params(fv, 768)
             for _ in range(12):
                 srv.submit("sedov", p, 60)
