@@ -390,7 +390,7 @@ def main():
     value = world * cells * args.steps / (ms_max * 1e-3)
     ms_step = ms_max / args.steps
 
-    # roofline of the fused step kernel (one launch per iteration)
+    # roofline of the fused step kernel (one step launch + a one-thread commit per iteration)
     peak, peak_kind = measured_peaks()
     achieved = BYTES_PER_CELL * cells / (ms_step * 1e-3) / 1e9
     prof = profile_figures()
@@ -476,7 +476,7 @@ def main():
                      "bytes_per_cell": BYTES_PER_CELL, "kernel": "fv2d::step_kernel<PLM,HLLC>"},
         "roofline_fp64": fp64,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-        "gpu_launches": args.steps + 1,
+        "gpu_launches": 2 * args.steps + 1,  # begin_kernel, then step_kernel + commit_kernel per iteration
         "sim_time": t_sim,
         "served": served,
     }

@@ -36,7 +36,7 @@ def _nvcc():
 # (source, extra flags)
 UNITS = [
     ("fv2d_api.cu", ["-fmad=false"]),
-    ("step_dispatch.cu", []),
+    ("step_dispatch.cu", ["-fmad=false"]),
     ("step_hll.cu", ["-fmad=false"]),
     ("step_hllc.cu", ["-fmad=false"]),
     ("step_fslp.cu", ["-fmad=false"]),

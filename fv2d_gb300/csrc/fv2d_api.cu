@@ -28,6 +28,7 @@ namespace fv2d {
 cudaError_t init_step_kernels();
 cudaError_t launch_step(int rs, int recon, dim3 grid, cudaStream_t s, const CUtensorMap &t0, const CUtensorMap &t1,
                         const StepArgs &a);
+cudaError_t launch_commit(cudaStream_t s, const StepArgs &a);
 }
 
 using namespace fv2d;
@@ -301,6 +302,7 @@ int launch_update(fv2d_ctx *ctx, int driven, double dt) {
     a.stage = STAGE_RK2_CORRECT;
     CK(launch_step(ctx->p.riemann_solver, rk, grid, ctx->stream, ctx->tm[0], ctx->tm[1], a));
   }
+  CK(launch_commit(ctx->stream, a));
   return FV2D_OK;
 }
 

@@ -14,7 +14,7 @@ constexpr int TY = 16;  // cells along y
 constexpr int HALO = 2; // ghost depth read by PLM + the 3x3 viscous stencil
 constexpr int SW = TX + 2 * HALO;  // staged tile width  (TMA box x)
 constexpr int SH = TY + 2 * HALO;  // staged tile height (TMA box y)
-constexpr int NT = 256;            // threads per CTA
+constexpr int NT = 288;            // threads per CTA (9 warps: the 544 faces of a tile in two rounds)
 
 enum { RECON_PCM = 0, RECON_PLM = 2, RECON_MH = 3 };
 enum { STAGE_EULER = 0, STAGE_RK2_PREDICT = 1, STAGE_RK2_CORRECT = 2 };

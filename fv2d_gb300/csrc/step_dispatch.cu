@@ -1,6 +1,6 @@
 // step_dispatch.cu -- selects the fused-step instantiation for a
 // (Riemann solver, reconstruction) pair.
-#include "step_common.cuh"
+#include "step_kernel.cuh"
 
 namespace fv2d {
 
@@ -29,6 +29,11 @@ cudaError_t launch_step(int rs, int recon, dim3 grid, cudaStream_t s, const CUte
     case 2: return launch_step_fslp(recon, grid, s, t0, t1, a);
     default: return launch_step_hllc(recon, grid, s, t0, t1, a);
   }
+}
+
+cudaError_t launch_commit(cudaStream_t s, const StepArgs &a) {
+  commit_kernel<<<1, 1, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 }  // namespace fv2d

@@ -19,8 +19,10 @@
 //      cell that copies it (BoundaryConditions.h:82-147, inverse map), and
 //      folds the next step's inverse hyperbolic dt (ComputeDt.h:26-52) into a
 //      warp-shuffle max and one atomic per CTA;
-//   6. the last CTA to finish commits t += dt, the counters and the next dt,
-//      and evaluates the device-driven loop condition (main.cpp:62-64).
+//   6. a one-thread kernel that follows in stream order commits t += dt, the
+//      counters and the next dt, and evaluates the device-driven loop
+//      condition (main.cpp:62-64); the step's CTAs only fire their reduction
+//      atomics and exit (no fence, no last-CTA election).
 // Built with -fmad=false the results are bit-identical to the reference's
 // binary64 arithmetic.
 #pragma once
@@ -118,7 +120,6 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
   __shared__ __align__(8) uint64_t mbar;
   __shared__ double red_max[NT / 32];
   __shared__ unsigned red_cnt[3][NT / 32];
-  __shared__ int s_last;
 
   DevState *st = a.st;
   const int tid = threadIdx.x;
@@ -501,23 +502,27 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
       c1 += red_cnt[1][w];
       c2 += red_cnt[2][w];
     }
+    // reductions only (no value returned, no fence): the commit kernel that
+    // follows in stream order reads the totals
     if (m >= 0.0) atomicMax(&st->acc_hyp, (unsigned long long)__double_as_longlong(m));
     if (c0) atomicAdd(&st->cnt_acc[0], (unsigned long long)c0);
     if (c1) atomicAdd(&st->cnt_acc[1], (unsigned long long)c1);
     if (c2) atomicAdd(&st->cnt_acc[2], (unsigned long long)c2);
-    __threadfence();
-    const unsigned t = atomicAdd(&st->ticket, 1u);
-    s_last = (t == (unsigned)a.nblocks - 1u);
   }
-  __syncthreads();
-  if (!s_last || tid != 0) return;
+}
 
-  // ---- 6. last CTA: commit the step -----------------------------------------
-  __threadfence();
+// ---- 6. commit the step (one thread, after the step kernel in stream order):
+// t += dt, the counters, the next dt, the per-iteration log and the
+// device-driven loop condition (main.cpp:62-64, 83; ComputeDt.h:64).
+static __global__ void commit_kernel(const StepArgs a) {
+  DevState *st = a.st;
   volatile DevState *vs = st;
+  if (a.driven && vs->status != RUN_RUNNING) return;
+  const int par = vs->parity;
+  const double dt = a.driven ? vs->dt : a.dt_arg;
   const double inv_prev = vs->inv_hyp;
   const double t_before = vs->t;
-  const double inv_hyp = __longlong_as_double((long long)atomicAdd(&st->acc_hyp, 0ull));
+  const double inv_hyp = __longlong_as_double((long long)vs->acc_hyp);
   double m = inv_hyp;  // std::max({hyp, tc, visc}) (ComputeDt.h:64)
   if (m < a.inv_tc) m = a.inv_tc;
   if (m < a.inv_visc) m = a.inv_visc;
@@ -532,7 +537,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
   if (a.stage == STAGE_EULER) vs->parity = 1 - par;
   unsigned long long cnt[3];
   for (int k = 0; k < 3; ++k) {
-    cnt[k] = atomicAdd(&st->cnt_acc[k], 0ull);
+    cnt[k] = vs->cnt_acc[k];
     vs->counters[k] = cnt[k];
     st->cnt_acc[k] = 0ull;
   }
@@ -560,8 +565,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
       s = RUN_PAUSED;
     vs->status = s;
   }
-  __threadfence();
-  st->ticket = 0u;
 }
+
 
 }  // namespace fv2d
