@@ -303,6 +303,12 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
   double *Qd = a.Q[dst];
   const long long PL = a.plane;
   const int P = a.pitch;
+  // dt/dx and dt/dy of the conduction update (ThermalConduction.h:106), once per CTA
+  double tc_dtdx = 0.0, tc_dtdy = 0.0;
+  if (a.tc) {
+    tc_dtdx = fv_div(dt, a.dx);
+    tc_dtdy = fv_div(dt, a.dy);
+  }
 
 #pragma unroll 1
   for (int cidx = tid; cidx < TX * TY; cidx += NT) {
@@ -381,8 +387,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         else
           FRt = kR * a.bctc_ymax_value;
       }
-      const double dtdx = fv_div(dt, a.dx), dtdy = fv_div(dt, a.dy);
-      un[3] += dtdx * (FRt - FLt) + dtdy * (FDt - FUt);
+      un[3] += tc_dtdx * (FRt - FLt) + tc_dtdy * (FDt - FUt);
     }
     // viscosity (Viscosity.h:148-228)
     if (a.visc) {
@@ -399,8 +404,8 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         const double sign = (side == 1 ? -1.0 : 1.0);
         const int s = side - 1, sm1 = side - 2;  // stencil index - 1
         {  // x faces
-          const double qiu = (U_(0, s) + U_(0, sm1)) * 0.5;
-          const double qiv = (V_(0, s) + V_(0, sm1)) * 0.5;
+          const double qiu = fv_half(U_(0, s) + U_(0, sm1));
+          const double qiv = fv_half(V_(0, s) + V_(0, sm1));
           const double dudx = odx * (U_(0, s) - U_(0, sm1));
           const double dvdx = odx * (V_(0, s) - V_(0, sm1));
           const double dudy = 0.25 * ody * (U_(1, s) - U_(-1, s) + U_(1, sm1) - U_(-1, sm1));
@@ -412,8 +417,8 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
           fx3 += sign * mu * (tau_xx * qiu + tau_xy * qiv);
         }
         {  // y faces
-          const double qiu = (U_(s, 0) + U_(sm1, 0)) * 0.5;
-          const double qiv = (V_(s, 0) + V_(sm1, 0)) * 0.5;
+          const double qiu = fv_half(U_(s, 0) + U_(sm1, 0));
+          const double qiv = fv_half(V_(s, 0) + V_(sm1, 0));
           const double dudy = ody * (U_(s, 0) - U_(sm1, 0));
           const double dvdy = ody * (V_(s, 0) - V_(sm1, 0));
           const double dudx = 0.25 * odx * (U_(s, 1) - U_(s, -1) + U_(sm1, 1) - U_(sm1, -1));
