@@ -35,7 +35,9 @@ __host__ __device__ __forceinline__ float fv_div(float a, float b) { return a / 
 // a1 / b and a2 / b (one reciprocal of b on the device)
 __host__ __device__ __forceinline__ void fv_div2(double a1, double a2, double b, double &q1, double &q2) {
 #ifdef __CUDA_ARCH__
-  softfp::div2_rn(a1, a2, b, q1, q2);
+  const double2 q = softfp::div2_rn(a1, a2, b);
+  q1 = q.x;
+  q2 = q.y;
 #else
   q1 = a1 / b;
   q2 = a2 / b;

@@ -67,8 +67,9 @@ __global__ void selftest_kernel(int op, uint64_t n, uint64_t seed, unsigned long
       h = a / b;
       s = sf::div_rn(a, b);
       const double c = ((r3 >> 56) & 3) == 0 ? 0.0 : operand(r2, r0, mode);
-      double s1;
-      sf::div2_rn(a, c, b, s1, s2);
+      const double2 q2 = sf::div2_rn(a, c, b);
+      const double s1 = q2.x;
+      s2 = q2.y;
       h2 = c / b;
       if (__double_as_longlong(s1) != __double_as_longlong(s) && !(s1 != s1 && s != s)) s2 = h2 + 1.0;
     } else if (op == 1) {

@@ -161,12 +161,12 @@ static __device__ __noinline__ double div_rn(double a, double b) {
   return div_finish(o, a, b, v);
 }
 
-// a1 / b and a2 / b
-static __device__ __noinline__ void div2_rn(double a1, double a2, double b, double &q1, double &q2) {
+// {a1 / b, a2 / b} (returned by value: outputs through references would live
+// on the stack across the call)
+static __device__ __noinline__ double2 div2_rn(double a1, double a2, double b) {
   const DivOp o1 = div_begin(a1, b), o2 = div_begin(a2, b);
   const uint64_t v = (o1.fast || o2.fast) ? recip_word(o1.d) : 0ull;
-  q1 = div_finish(o1, a1, b, v);
-  q2 = div_finish(o2, a2, b, v);
+  return make_double2(div_finish(o1, a1, b, v), div_finish(o2, a2, b, v));
 }
 
 // sqrt(x), round to nearest even.

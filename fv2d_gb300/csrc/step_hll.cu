@@ -4,31 +4,46 @@
 
 namespace fv2d {
 
+namespace {
+template <int RECON, bool VISC>
+cudaError_t attr() {
+  return cudaFuncSetAttribute(step_kernel<RECON, RS_HLL, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)Smem<RECON, VISC>::BYTES);
+}
+template <bool VISC>
+void launch(int recon, dim3 grid, cudaStream_t s, const CUtensorMap &t0, const CUtensorMap &t1, const StepArgs &a) {
+  switch (recon) {
+    case RECON_PLM:
+      step_kernel<RECON_PLM, RS_HLL, VISC><<<grid, NT, Smem<RECON_PLM, VISC>::BYTES, s>>>(t0, t1, a);
+      break;
+    case RECON_MH:
+      step_kernel<RECON_MH, RS_HLL, VISC><<<grid, NT, Smem<RECON_MH, VISC>::BYTES, s>>>(t0, t1, a);
+      break;
+    default:
+      step_kernel<RECON_PCM, RS_HLL, VISC><<<grid, NT, Smem<RECON_PCM, VISC>::BYTES, s>>>(t0, t1, a);
+      break;
+  }
+}
+}  // namespace
+
 cudaError_t set_step_attrs_hll() {
-  cudaError_t e = cudaFuncSetAttribute(step_kernel<RECON_PCM, RS_HLL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)Smem<RECON_PCM>::BYTES);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(step_kernel<RECON_PLM, RS_HLL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)Smem<RECON_PLM>::BYTES);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(step_kernel<RECON_MH, RS_HLL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)Smem<RECON_MH>::BYTES);
+  cudaError_t e = attr<RECON_PCM, false>();
+  if (e == cudaSuccess) e = attr<RECON_PLM, false>();
+  if (e == cudaSuccess) e = attr<RECON_MH, false>();
+  if (e == cudaSuccess) e = attr<RECON_PCM, true>();
+  if (e == cudaSuccess) e = attr<RECON_PLM, true>();
+  if (e == cudaSuccess) e = attr<RECON_MH, true>();
   return e;
 }
 
+// the viscous terms are a separate instantiation: kernels without them keep
+// their registers and shared memory
 cudaError_t launch_step_hll(int recon, dim3 grid, cudaStream_t s, const CUtensorMap &t0, const CUtensorMap &t1,
                             const StepArgs &a) {
-  switch (recon) {
-    case RECON_PLM:
-      step_kernel<RECON_PLM, RS_HLL><<<grid, NT, Smem<RECON_PLM>::BYTES, s>>>(t0, t1, a);
-      break;
-    case RECON_MH:
-      step_kernel<RECON_MH, RS_HLL><<<grid, NT, Smem<RECON_MH>::BYTES, s>>>(t0, t1, a);
-      break;
-    default:
-      step_kernel<RECON_PCM, RS_HLL><<<grid, NT, Smem<RECON_PCM>::BYTES, s>>>(t0, t1, a);
-      break;
-  }
+  if (a.visc)
+    launch<true>(recon, grid, s, t0, t1, a);
+  else
+    launch<false>(recon, grid, s, t0, t1, a);
   return cudaGetLastError();
 }
 

@@ -91,8 +91,9 @@ __device__ __forceinline__ double warp_max_nonneg(double v) {
 }
 __device__ __forceinline__ unsigned warp_sum(unsigned v) { return __reduce_add_sync(0xffffffffu, v); }
 
-// Shared-memory layout (in doubles) for a reconstruction type.
-template <int RECON>
+// Shared-memory layout (in doubles) for a reconstruction type, with or
+// without the viscous face terms.
+template <int RECON, bool VISC = false>
 struct Smem {
   static constexpr int R1W = TX + 2, R1H = TY + 2;  // tile + 1-cell ring
   static constexpr int R1 = R1W * R1H;
@@ -104,21 +105,24 @@ struct Smem {
   static constexpr int FY = FX + 4 * TY * (TX + 1);
   static constexpr int PY = FY + 4 * (TY + 1) * TX;
   static constexpr int T = PY + (TY + 1) * TX;
-  static constexpr int TOTAL = T + R1;
+  static constexpr int VX = T + R1;                                  // viscous x-face terms, 3 x TY x (TX+1)
+  static constexpr int VY = VX + (VISC ? 3 * TY * (TX + 1) : 0);     // viscous y-face terms, 3 x (TY+1) x TX
+  static constexpr int TOTAL = VY + (VISC ? 3 * (TY + 1) * TX : 0);
   static constexpr size_t BYTES = sizeof(double) * TOTAL + 128;  // + alignment slack
 };
 
-template <int RECON, int RS>
+template <int RECON, int RS, bool VISC>
 __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     step_kernel(const __grid_constant__ CUtensorMap tmQ0, const __grid_constant__ CUtensorMap tmQ1,
                 const StepArgs a) {
-  using L = Smem<RECON>;
+  using L = Smem<RECON, VISC>;
   // Aligned by offsetting the shared array itself (not through an integer
   // round trip, which would turn every tile access into a generic load).
   extern __shared__ __align__(128) unsigned char fv2d_step_smem[];
   double *sm = reinterpret_cast<double *>(fv2d_step_smem + ((128u - ((uint32_t)__cvta_generic_to_shared(fv2d_step_smem) & 127u)) & 127u));
   __shared__ __align__(8) uint64_t mbar;
   __shared__ double red_max[NT / 32];
+  __shared__ double s_tc[2];  // dt/dx, dt/dy of the conduction update (ThermalConduction.h:106), once per CTA
   __shared__ unsigned red_cnt[3][NT / 32];
 
   DevState *st = a.st;
@@ -213,6 +217,10 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
       const int ly = it / L::R1W + 1, lx = it % L::R1W + 1;
       sR1(L::T, 0, ly, lx) = fv_div(sQ(3, ly, lx), sQ(0, ly, lx));
     }
+    if (tid == NT - 1) {
+      s_tc[0] = fv_div(dt, a.dx);
+      s_tc[1] = fv_div(dt, a.dy);
+    }
   }
   __syncthreads();
   if constexpr (RECON == RECON_MH) {
@@ -292,6 +300,54 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
       }
     }
   }
+  // viscous face terms (Viscosity.h:148-228), once per face: the two cells of
+  // a face evaluate the same expressions in the reference, the one on the
+  // +side of the face with sign -1, which only negates the products exactly
+  if constexpr (VISC) {
+    constexpr double four_thirds = 4.0 / 3.0;
+    constexpr double two_thirds = 2.0 / 3.0;
+    const double mu = a.mu;
+    const double odx = a.one_over_dx, ody = a.one_over_dy;
+    constexpr int NVX = TY * (TX + 1), NVY = (TY + 1) * TX;
+    for (int f = tid; f < NVX + NVY; f += NT) {
+      if (f < NVX) {  // between columns c+1 (s-1) and c+2 (s) of row r+2
+        const int r = f / (TX + 1), c = f % (TX + 1);
+        const int ly = r + 2, xs = c + 2, xm = c + 1;
+        auto U_ = [&](int dj, int x) { return sQ(1, ly + dj, x); };
+        auto V_ = [&](int dj, int x) { return sQ(2, ly + dj, x); };
+        const double qiu = fv_half(U_(0, xs) + U_(0, xm));
+        const double qiv = fv_half(V_(0, xs) + V_(0, xm));
+        const double dudx = odx * (U_(0, xs) - U_(0, xm));
+        const double dvdx = odx * (V_(0, xs) - V_(0, xm));
+        const double dudy = 0.25 * ody * (U_(1, xs) - U_(-1, xs) + U_(1, xm) - U_(-1, xm));
+        const double dvdy = 0.25 * ody * (V_(1, xs) - V_(-1, xs) + V_(1, xm) - V_(-1, xm));
+        const double tau_xx = four_thirds * dudx - two_thirds * dvdy;
+        const double tau_xy = dvdx + dudy;
+        double *Vf = sm + L::VX + f;
+        Vf[0] = mu * tau_xx;
+        Vf[NVX] = mu * tau_xy;
+        Vf[2 * NVX] = mu * (tau_xx * qiu + tau_xy * qiv);
+      } else {  // between rows r+1 (s-1) and r+2 (s) of column c+2
+        const int g = f - NVX;
+        const int r = g / TX, c = g % TX;
+        const int lx = c + 2, ys = r + 2, ym = r + 1;
+        auto U_ = [&](int y, int di) { return sQ(1, y, lx + di); };
+        auto V_ = [&](int y, int di) { return sQ(2, y, lx + di); };
+        const double qiu = fv_half(U_(ys, 0) + U_(ym, 0));
+        const double qiv = fv_half(V_(ys, 0) + V_(ym, 0));
+        const double dudy = ody * (U_(ys, 0) - U_(ym, 0));
+        const double dvdy = ody * (V_(ys, 0) - V_(ym, 0));
+        const double dudx = 0.25 * odx * (U_(ys, 1) - U_(ys, -1) + U_(ym, 1) - U_(ym, -1));
+        const double dvdx = 0.25 * odx * (V_(ys, 1) - V_(ys, -1) + V_(ym, 1) - V_(ym, -1));
+        const double tau_yy = four_thirds * dvdy - two_thirds * dudx;
+        const double tau_xy = dvdx + dudy;
+        double *Vf = sm + L::VY + g;
+        Vf[0] = mu * tau_xy;
+        Vf[NVY] = mu * tau_yy;
+        Vf[2 * NVY] = mu * (tau_xy * qiu + tau_yy * qiv);
+      }
+    }
+  }
   __syncthreads();
 
   // ---- 4./5. cell update, conversion, stores, reductions -------------------
@@ -303,12 +359,6 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
   double *Qd = a.Q[dst];
   const long long PL = a.plane;
   const int P = a.pitch;
-  // dt/dx and dt/dy of the conduction update (ThermalConduction.h:106), once per CTA
-  double tc_dtdx = 0.0, tc_dtdy = 0.0;
-  if (a.tc) {
-    tc_dtdx = fv_div(dt, a.dx);
-    tc_dtdy = fv_div(dt, a.dy);
-  }
 
 #pragma unroll 1
   for (int cidx = tid; cidx < TX * TY; cidx += NT) {
@@ -387,49 +437,27 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         else
           FRt = kR * a.bctc_ymax_value;
       }
-      un[3] += tc_dtdx * (FRt - FLt) + tc_dtdy * (FDt - FUt);
+      un[3] += s_tc[0] * (FRt - FLt) + s_tc[1] * (FDt - FUt);
     }
-    // viscosity (Viscosity.h:148-228)
-    if (a.visc) {
-      constexpr double four_thirds = 4.0 / 3.0;
-      constexpr double two_thirds = 2.0 / 3.0;
-      const double mu = a.mu;
-      const double odx = a.one_over_dx, ody = a.one_over_dy;
-      // stencil[dj+1][di+1] = Q(i+di, j+dj)
-      auto U_ = [&](int dj, int di) { return sQ(1, ly + dj, lx + di); };
-      auto V_ = [&](int dj, int di) { return sQ(2, ly + dj, lx + di); };
+    // viscosity (Viscosity.h:148-228): the face terms of the face pass, the
+    // -side face negated, accumulated in the reference's order
+    if constexpr (VISC) {
+      constexpr int NVX = TY * (TX + 1), NVY = (TY + 1) * TX;
+      const double *Vw = sm + L::VX + ry * (TX + 1) + rx;  // x face at rx (west), rx + 1 (east)
+      const double *Vn = sm + L::VY + ry * TX + rx;        // y face at ry (north), ry + 1 (south)
       double fx1 = 0.0, fx2 = 0.0, fx3 = 0.0, fy1 = 0.0, fy2 = 0.0, fy3 = 0.0;
-#pragma unroll
-      for (int side = 1; side < 3; ++side) {
-        const double sign = (side == 1 ? -1.0 : 1.0);
-        const int s = side - 1, sm1 = side - 2;  // stencil index - 1
-        {  // x faces
-          const double qiu = fv_half(U_(0, s) + U_(0, sm1));
-          const double qiv = fv_half(V_(0, s) + V_(0, sm1));
-          const double dudx = odx * (U_(0, s) - U_(0, sm1));
-          const double dvdx = odx * (V_(0, s) - V_(0, sm1));
-          const double dudy = 0.25 * ody * (U_(1, s) - U_(-1, s) + U_(1, sm1) - U_(-1, sm1));
-          const double dvdy = 0.25 * ody * (V_(1, s) - V_(-1, s) + V_(1, sm1) - V_(-1, sm1));
-          const double tau_xx = four_thirds * dudx - two_thirds * dvdy;
-          const double tau_xy = dvdx + dudy;
-          fx1 += sign * mu * tau_xx;
-          fx2 += sign * mu * tau_xy;
-          fx3 += sign * mu * (tau_xx * qiu + tau_xy * qiv);
-        }
-        {  // y faces
-          const double qiu = fv_half(U_(s, 0) + U_(sm1, 0));
-          const double qiv = fv_half(V_(s, 0) + V_(sm1, 0));
-          const double dudy = ody * (U_(s, 0) - U_(sm1, 0));
-          const double dvdy = ody * (V_(s, 0) - V_(sm1, 0));
-          const double dudx = 0.25 * odx * (U_(s, 1) - U_(s, -1) + U_(sm1, 1) - U_(sm1, -1));
-          const double dvdx = 0.25 * odx * (V_(s, 1) - V_(s, -1) + V_(sm1, 1) - V_(sm1, -1));
-          const double tau_yy = four_thirds * dvdy - two_thirds * dudx;
-          const double tau_xy = dvdx + dudy;
-          fy1 += sign * mu * tau_xy;
-          fy2 += sign * mu * tau_yy;
-          fy3 += sign * mu * (tau_xy * qiu + tau_yy * qiv);
-        }
-      }
+      fx1 += -Vw[0];
+      fx2 += -Vw[NVX];
+      fx3 += -Vw[2 * NVX];
+      fy1 += -Vn[0];
+      fy2 += -Vn[NVY];
+      fy3 += -Vn[2 * NVY];
+      fx1 += Vw[1];
+      fx2 += Vw[NVX + 1];
+      fx3 += Vw[2 * NVX + 1];
+      fy1 += Vn[TX];
+      fy2 += Vn[NVY + TX];
+      fy3 += Vn[2 * NVY + TX];
       un[0] += (0.0 + 0.0) * dt;
       un[1] += (fx1 + fy1) * dt;
       un[2] += (fx2 + fy2) * dt;
