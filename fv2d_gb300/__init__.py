@@ -71,6 +71,7 @@ def lib():
         L.fv2d_probe_fp64_peak.argtypes = [C.c_int, _dp]
         L.fv2d_compute_dt_noalloc.argtypes = [C.POINTER(Params), vp, vp, vp]
         L.fv2d_selftest_arith.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64), _dp]
+        L.fv2d_selftest_wait_timeout.argtypes = [C.c_uint32, C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -97,6 +98,16 @@ def probe_fp64_peak(device=0):
     if rc != 0:
         raise Fv2dError(rc, "fp64 probe failed")
     return g.value
+
+
+def selftest_wait_timeout(limit=1000):
+    """Error bits set by a bounded device wait on a barrier that is never
+    completed (1 = timed out and returned)."""
+    flag = C.c_int()
+    rc = lib().fv2d_selftest_wait_timeout(int(limit), C.byref(flag))
+    if rc != 0:
+        raise Fv2dError(rc, "wait self-test failed to run")
+    return flag.value
 
 
 def selftest_arith(op, n, seed=1):

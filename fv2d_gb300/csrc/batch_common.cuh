@@ -38,7 +38,7 @@ struct __align__(64) SimDev {
   unsigned int ticket;    // tiles finished in the running launch
   unsigned long long negatives;  // cells reset by the negative guard (all steps)
   int tma_ok;           // tensor map valid for this simulation
-  int pad0;
+  unsigned int nan_cells;  // NaN cells produced by the running step: the commit fails the simulation
 };
 
 // Pressure (E - rho |u|^2 / 2)(gamma - 1) of the binary32 state.  Low-Mach
@@ -54,6 +54,8 @@ __device__ __forceinline__ float pressure_of(float E, float r, float u, float v,
   }
   return (E - ek) * gm1;
 }
+
+__device__ __forceinline__ bool is_nan_f(float x) { return (__float_as_uint(x) & 0x7FFFFFFFu) > 0x7F800000u; }
 
 // A tile of one simulation: sim index in the table, tile coordinates.
 struct WorkItem {

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
   __shared__ __align__(8) uint64_t mbar;
   __shared__ float red_max[NT / 32];
   __shared__ unsigned red_neg[NT / 32];
+  __shared__ unsigned red_nan[NT / 32];
   __shared__ int s_last;
   const int tid = threadIdx.x;
   uint32_t phase = 0;
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
 
     // ---- update, store, reductions --------------------------------------------
     float lmax = 0.f;
-    unsigned nneg = 0;
+    unsigned nneg = 0, nnan = 0;
     const float dtdx = dt * S.inv_dx, dtdy = dt * S.inv_dy;
     for (int cidx = tid; cidx < TX * TY; cidx += NT) {
       const int ry = cidx / TX, rx = cidx % TX;
@@ -302,6 +303,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
       // primitive state of the new cell for the next dt
       float r = un[0], u = un[1] / r, v = un[2] / r;
       float p = pressure_of(un[3], r, u, v, S.gm1, S.lowmach);
+      nnan += is_nan_f(r) | is_nan_f(u) | is_nan_f(v) | is_nan_f(p);
       nneg += (r < 0.f) + (p < 0.f);
       if (r < 0.f) r = 1e-8f;
       if (p < 0.f) p = 1e-8f;
@@ -332,21 +334,25 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
     const unsigned wn = __reduce_add_sync(0xffffffffu, nneg);
+    const unsigned wnan = __reduce_add_sync(0xffffffffu, nnan);
     if ((tid & 31) == 0) {
       red_max[tid >> 5] = lmax;
       red_neg[tid >> 5] = wn;
+      red_nan[tid >> 5] = wnan;
     }
     __syncthreads();
     if (tid == 0) {
       float m = 0.f;
-      unsigned n = 0;
+      unsigned n = 0, nn = 0;
       for (int k = 0; k < NT / 32; ++k) {
         m = fmaxf(m, red_max[k]);
         n += red_neg[k];
+        nn += red_nan[k];
       }
       SimDev *G = &a.sims[item.sim];
       atomicMax(&G->acc_bits, __float_as_uint(m));
       if (n) atomicAdd(&G->negatives, (unsigned long long)n);
+      if (nn) atomicAdd(&G->nan_cells, nn);
       __threadfence();
       const unsigned t = atomicAdd(&G->ticket, 1u);
       s_last = (t == (unsigned)(S.ntx * S.nty) - 1u);
@@ -369,11 +375,12 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
       G->dt = dtn;
       G->acc_bits = 0u;
       int status = SIM_ACTIVE;
-      if (!(dtn > 0.0) || isinf(dtn))
+      if (!(dtn > 0.0) || isinf(dtn) || G->nan_cells)  // the NaN / dt guard fails this request only
         status = SIM_FAILED;
       else if (step >= S.max_steps || !(t + S.eps < S.tend))
         status = SIM_DONE;
       G->status = status;
+      G->nan_cells = 0u;
       __threadfence();
       G->ticket = 0u;
     }

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a
     S4<float> Gm = yflux(add4(qm, hm), sub4(q0, h0), S, gas);
 
     float lmax = 0.f;
-    unsigned nneg = 0;
+    unsigned nneg = 0, nnan = 0;
     // rows are loaded one iteration ahead of their use: the loads of row
     // C + 3 are in flight while row C is computed
     float Unext[4];
@@ -253,6 +253,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a
         // primitive state of the new cell for the next dt
         float r = un[0], u = un[1] / r, v = un[2] / r;
         float p = pressure_of(un[3], r, u, v, S.gm1, S.lowmach);
+        nnan += is_nan_f(r) | is_nan_f(u) | is_nan_f(v) | is_nan_f(p);
         nneg += (r < 0.f) + (p < 0.f);
         if (r < 0.f) r = 1e-8f;
         if (p < 0.f) p = 1e-8f;
@@ -297,10 +298,12 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
     const unsigned wn = __reduce_add_sync(0xffffffffu, nneg);
+    const unsigned wnan = __reduce_add_sync(0xffffffffu, nnan);
     if (lane == 0) {
       SimDev *Gw = a.sims + item.sim;
       atomicMax(&Gw->acc_bits, __float_as_uint(lmax));
       if (wn) atomicAdd(&Gw->negatives, (unsigned long long)wn);
+      if (wnan) atomicAdd(&Gw->nan_cells, wnan);
       __threadfence();
       const unsigned t = atomicAdd(&Gw->ticket, 1u);
       if (t == (unsigned)(G->ntx * G->nty) - 1u) {
@@ -320,11 +323,12 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a
         V->dt = dtn;
         V->acc_bits = 0u;
         int status = SIM_ACTIVE;
-        if (!(dtn > 0.0) || isinf(dtn))
+        if (!(dtn > 0.0) || isinf(dtn) || V->nan_cells)  // the NaN / dt guard fails this request only
           status = SIM_FAILED;
         else if (step >= V->max_steps || !(t_new + V->eps < V->tend))
           status = SIM_DONE;
         V->status = status;
+        V->nan_cells = 0u;
         __threadfence();
         V->ticket = 0u;
       }

@@ -6,6 +6,7 @@
 
 #include "../../include/fv2d_gpu.h"
 #include "softfp.cuh"
+#include "step_kernel.cuh"
 
 namespace {
 
@@ -144,5 +145,33 @@ extern "C" int fv2d_selftest_arith(int op, uint64_t n, uint64_t seed, uint64_t *
   *mismatches = h;
   if (example)
     for (int k = 0; k < 3; ++k) example[k] = hx[k];
+  return FV2D_OK;
+}
+
+namespace {
+// A wait that nothing will end: an mbarrier expecting one arrival that never
+// comes, waited on with the step kernel's bounded wait.
+__global__ void wait_timeout_kernel(uint32_t limit, int *flag) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    fv2d::mbar_init(&bar, 1);
+    fv2d::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) fv2d::mbar_wait_bounded(&bar, flag, limit);
+}
+}  // namespace
+
+extern "C" int fv2d_selftest_wait_timeout(uint32_t limit, int *timed_out) {
+  if (!timed_out || limit == 0 || limit > (1u << 20)) return FV2D_ERR_INVALID;
+  int *flag = nullptr;
+  if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) return FV2D_ERR_NOMEM;
+  cudaMemset(flag, 0, sizeof(int));
+  wait_timeout_kernel<<<1, 32>>>(limit, flag);
+  int h = 0;
+  const cudaError_t e = cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(flag);
+  if (e != cudaSuccess) return FV2D_ERR_CUDA;
+  *timed_out = h;
   return FV2D_OK;
 }

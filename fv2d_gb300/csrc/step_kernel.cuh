@@ -68,11 +68,11 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
 // Bounded wait on phase 0 of a one-shot barrier.  Gives up after ~seconds,
 // records the error and waits (again bounded) so that no copy is left in
 // flight into shared memory when the CTA exits.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err_flag) {
-  for (uint32_t it = 0; it < (1u << 24); ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err_flag, uint32_t limit = 1u << 24) {
+  for (uint32_t it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, 0)) return true;
   atomicOr(err_flag, DEVERR_TMA_TIMEOUT);
-  for (uint32_t it = 0; it < (1u << 24); ++it)
+  for (uint32_t it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, 0)) break;
   return false;
 }

@@ -178,6 +178,13 @@ int fv2d_compute_dt_noalloc(const fv2d_params *p, const double *q_dev, double *o
  * example receives {a, b, integer result} of the first mismatch. */
 int fv2d_selftest_arith(int op, uint64_t n, uint64_t seed, uint64_t *mismatches, double example[3]);
 
+/* Self-test of the device-side wait guard (no reference counterpart): one
+ * thread waits, with the step kernel's bounded wait and an iteration limit of
+ * `limit` (1 .. 2^20), on a barrier that is never completed.  *timed_out
+ * receives the error bits the wait sets (DEVERR_TMA_TIMEOUT = 1) instead of
+ * hanging; the context stays usable afterwards. */
+int fv2d_selftest_wait_timeout(uint32_t limit, int *timed_out);
+
 /* sizeof(fv2d_params) as compiled into the library. */
 size_t fv2d_params_size(void);
 

@@ -230,3 +230,37 @@ def test_readers_parse_a_libhdf5_file(L):
     out = np.empty(64)
     assert L.fv2d_h5_read_doubles(f.encode(), b"/testdouble", _dp(out), 64, C.byref(n)) == 0
     assert n.value == 9 and np.array_equal(out[:9], ref)
+
+
+def test_damaged_snapshot_files_are_reported_not_read(L, tmp_path):
+    """A restart from a truncated, overwritten or non-HDF5 file returns an
+    error code and a message; it never reads past the file or crashes."""
+    nx, ny = 12, 7
+    p = fv.default_params(Nx=nx, Ny=ny)
+    q = np.random.default_rng(5).uniform(0.1, 2.0, (ny, nx, 4))
+    write(L, tmp_path, "run", 0, 1, p, "blast", 0, 0.0, q)
+    good = tmp_path / "run.h5"
+    data = good.read_bytes()
+    cases = {
+        "empty.h5": b"",
+        "text.h5": b"not an hdf5 file\n" * 40,
+        "sig_only.h5": data[:8],
+    }
+    for frac in (0.1, 0.3, 0.5, 0.8, 0.95):
+        cases[f"cut{int(frac * 100)}.h5"] = data[:int(len(data) * frac)]
+    rng = np.random.default_rng(9)
+    for k in range(4):  # random bytes overwritten after the superblock
+        b = bytearray(data)
+        pos = rng.integers(64, len(b), 32)
+        for i in pos:
+            b[i] = int(rng.integers(0, 256))
+        cases[f"noise{k}.h5"] = bytes(b)
+    for name, blob in cases.items():
+        f = tmp_path / name
+        f.write_bytes(blob)
+        rc, _, _, _, err = read(L, str(f) + ":/ite_0000", nx, ny)
+        if name.startswith("noise") and rc == 0:
+            continue  # the overwritten bytes may have missed every structure that is read
+        assert rc != 0 and err, name
+    rc, q2, t, it, err = read(L, str(good) + ":/ite_0000", nx, ny)
+    assert rc == 0 and np.array_equal(q2, q), err

@@ -124,3 +124,27 @@ def test_negative_reset_counters():
     c = o.counters()
     assert c[0] == 12 and c[2] == 0
     assert (o.get_prim()[..., 0] > 0).all()
+
+
+def test_sod_converges_to_the_exact_riemann_solution():
+    """Physics check of the scheme the oracle restates (and the GPU path
+    reproduces bit for bit): the Sod problem of the benchmark set-up against
+    the exact Riemann solution (tests/exact_riemann.py), in L1 for rho, u
+    and p, with the error shrinking as the grid is refined."""
+    import exact_riemann as ER
+    g = float(np.float32(1.4))
+    errs = {}
+    for nx in (128, 512):
+        p = reference_params(Nx=nx, Ny=8, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0 / 64, gamma0=1.4,
+                             reconstruction=2, riemann_solver=1, CFL=0.8, boundary_x=0, boundary_y=2, tend=0.2)
+        o = Oracle(p)
+        o.init_problem("sod_x")
+        t, _ = o.run(p.tend, 100000)
+        q = o.get_prim()
+        assert np.all(q == q[:1]), "rows of the y-uniform problem differ"
+        x = (np.arange(nx) + 0.5) / nx
+        rho, u, pr = ER.profile((1.0, 0.0, 1.0), (0.125, 0.0, 0.1), g, x, 0.5, t)
+        errs[nx] = [float(np.mean(np.abs(q[0, :, k] - ex))) for k, ex in ((0, rho), (1, u), (3, pr))]
+    print(errs)
+    assert all(e < 1e-2 for e in errs[512]), errs
+    assert all(errs[512][k] < 0.5 * errs[128][k] for k in range(3)), errs
