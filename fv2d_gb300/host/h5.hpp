@@ -1,6 +1,6 @@
 // h5.hpp -- the reference's HDF5 snapshot layout (IOManager.h:107-282) and
 // restart reading (IOManager.h:284-398), written and read without libhdf5
-// (not available to this build) from the published HDF5 file-format
+// (the library is not a dependency here) from the published HDF5 file-format
 // specification.
 //
 // Files written here use the classic format every HDF5 reader accepts:

@@ -11,7 +11,8 @@
  * floating-point operations, compiled with -ffp-contract=off.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
- * load this library, and only as the checker / the timed CPU baseline.
+ * load this library, and only as the oracle results are compared against or
+ * as the timed CPU baseline; the product path never calls it.
  *
  * Pinning: the restatement is checked against (1) the reference's only
  * published known answers (README.md:86-89, the blast.ini dt log) and
