@@ -23,6 +23,7 @@
 #include "problems.h"
 #include "step_common.cuh"
 #include "physics.cuh"
+#include "nvtx_range.h"
 
 namespace fv2d {
 cudaError_t init_step_kernels();
@@ -534,6 +535,7 @@ int fv2d_set_prim_device(fv2d_ctx *ctx, const double *q_dev) {
 }
 
 int fv2d_set_prim(fv2d_ctx *ctx, const double *q_host) {
+  const fv2d::NvtxRange nvtx_range("fv2d_set_prim");
   if (!ctx || !q_host) return FV2D_ERR_INVALID;
   // Page-locked host memory is read by the set-up kernel itself over the
   // host link (one pass instead of a copy then a pass); pageable memory is
@@ -566,6 +568,7 @@ int fv2d_set_host_mirror(fv2d_ctx *ctx, double *q_host) {
 }
 
 int fv2d_init_problem(fv2d_ctx *ctx, int problem) {
+  const fv2d::NvtxRange nvtx_range("fv2d_init_problem");
   if (!ctx) return FV2D_ERR_INVALID;
   if (!problem_valid(problem)) return fail(ctx, FV2D_ERR_INVALID, "unknown problem id");
   const fv2d_params &p = ctx->p;
@@ -591,6 +594,7 @@ static int get_planes(fv2d_ctx *ctx, const double *planes, double *dst, cudaMemc
 }
 
 int fv2d_get_prim(fv2d_ctx *ctx, double *q_host) {
+  const fv2d::NvtxRange nvtx_range("fv2d_get_prim");
   if (!ctx || !q_host) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   if (int rc = sync_state(ctx)) return rc;
@@ -612,6 +616,7 @@ int fv2d_get_cons(fv2d_ctx *ctx, double *u_host) {
 }
 
 int fv2d_compute_dt(fv2d_ctx *ctx, double *dt, double *inv_hyp, double *inv_tc, double *inv_visc) {
+  const fv2d::NvtxRange nvtx_range("fv2d_compute_dt");
   if (!ctx) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   if (int rc = sync_state(ctx)) return rc;
@@ -623,6 +628,7 @@ int fv2d_compute_dt(fv2d_ctx *ctx, double *dt, double *inv_hyp, double *inv_tc, 
 }
 
 int fv2d_update(fv2d_ctx *ctx, double dt) {
+  const fv2d::NvtxRange nvtx_range("fv2d_update");
   if (!ctx) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   ctx->mirror_valid = false;
@@ -658,6 +664,7 @@ int fv2d_set_time(fv2d_ctx *ctx, double t, int iteration) {
 
 int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, int skip_first_save_check, double *t,
                  int *steps_done, int *status) {
+  const fv2d::NvtxRange nvtx_range("fv2d_advance");
   if (!ctx) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   if (max_steps < 0) return fail(ctx, FV2D_ERR_INVALID, "max_steps < 0");
@@ -692,6 +699,7 @@ int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, in
 }
 
 int fv2d_run_async(fv2d_ctx *ctx, int n) {
+  const fv2d::NvtxRange nvtx_range("fv2d_run_async");
   if (!ctx || n < 0) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   ctx->mirror_valid = false;

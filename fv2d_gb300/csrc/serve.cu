@@ -33,6 +33,7 @@
 #include "ic.h"
 #include "physics.cuh"
 #include "problems.h"
+#include "nvtx_range.h"
 
 namespace fv2d {
 int batch_num_cfgs();
@@ -333,6 +334,7 @@ size_t state_bytes(int N, int *pitch, long long *plane) {
 // Admit one request into a free slot; returns the slot, or -1 when it does
 // not fit.
 int admit(fv2d_server *s, const Pending &pd) {
+  const NvtxRange nvtx_range("fv2d_server admit");
   if (s->free_slots.empty()) return -1;
   const fv2d_request &r = pd.req;
   const fv2d_params &p = r.params;
@@ -527,6 +529,7 @@ cudaGraphExec_t get_graph(fv2d_server *s, int K, int mask) {
 // state copies are queued for all of them, then one synchronisation.
 void retire_all(fv2d_server *s, const std::vector<int> &done) {
   if (done.empty()) return;
+  const NvtxRange nvtx_range("fv2d_server retire");
   size_t need = 0;
   std::vector<size_t> off(done.size());
   for (size_t k = 0; k < done.size(); ++k) {
@@ -604,6 +607,7 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
 // Replay K steps of every active simulation and retire the finished ones.
 // Returns false when nothing was active.
 bool run_once(fv2d_server *s, int K_fixed) {
+  const NvtxRange nvtx_range("fv2d_server replay");
   bool any = false;
   double active_cells = 0;
   for (int k = 0; k < s->max_sims; ++k)

@@ -1,4 +1,4 @@
-// driver.cpp -- fv2d_gpu <file.ini> [--device N]
+// driver.cpp -- fv2d_gpu <file.ini> [--device N] [--metrics FILE]
 //
 // The reference's executable (main.cpp:13-101) on the GB300 path: read the
 // .ini, echo it, initialise or restart, then run the main loop
@@ -6,8 +6,12 @@
 // with the iterations between snapshots executed on the device
 // (fv2d_advance) and the console lines of the reference (dt log every
 // log_frequency + 1 iterations, negative-value messages, save notices)
-// printed from the per-iteration device log.
+// printed from the per-iteration device log.  --metrics writes the same log
+// as JSON lines (one per iteration: t, dt, inverse dts, checkNegatives counts)
+// plus one line per device-driven batch with its wall time and throughput.
+#include <chrono>
 #include <climits>
+#include <fstream>
 #include <cstdio>
 #include <cstring>
 #include <filesystem>
@@ -64,10 +68,17 @@ void print_counters(double nd, double np, double nn) {
 }  // namespace
 
 int main(int argc, char **argv) {
-  if (argc < 2) return die("usage: fv2d_gpu <file.ini> [--device N]");
+  if (argc < 2) return die("usage: fv2d_gpu <file.ini> [--device N] [--metrics FILE]");
   int device = 0;
-  for (int k = 2; k + 1 < argc; ++k)
+  std::ofstream metrics;
+  for (int k = 2; k + 1 < argc; ++k) {
     if (std::string(argv[k]) == "--device") device = std::atoi(argv[k + 1]);
+    if (std::string(argv[k]) == "--metrics") {
+      metrics.open(argv[k + 1]);
+      if (!metrics) return die(std::string("cannot write ") + argv[k + 1]);
+      metrics.precision(17);
+    }
+  }
   std::cout << "fv2d on GB300 (binary64, bit-identical to the reference step)" << std::endl;
 
   Run r;
@@ -131,14 +142,29 @@ int main(int argc, char **argv) {
   int next_log = 0;
   bool resumed_after_save = false;
   std::vector<double> rec(6 * 4096);
+  long long step_no = 0;
   for (;;) {
     double td;
     int n, status;
+    const auto w0 = std::chrono::steady_clock::now();
     const int rc = fv2d_advance(r.ctx, 4096, r.p.tend, next_save, resumed_after_save ? 1 : 0, &td, &n, &status);
+    const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
     int got = 0;
     fv2d_get_step_log(r.ctx, rec.data(), 4096, &got);
     double itc = 0, iv = 0;
     fv2d_compute_dt(r.ctx, nullptr, nullptr, &itc, &iv);
+    if (metrics.is_open()) {
+      for (int k = 0; k < got; ++k, ++step_no) {
+        const double *e = &rec[6 * k];
+        metrics << "{\"step\": " << step_no << ", \"t\": " << e[0] << ", \"dt\": " << e[1] << ", \"inv_dt_hyp\": " << e[2]
+                << ", \"inv_dt_tc\": " << itc << ", \"inv_dt_visc\": " << iv << ", \"neg_rho\": " << (long long)e[3]
+                << ", \"neg_p\": " << (long long)e[4] << ", \"nan\": " << (long long)e[5] << "}\n";
+      }
+      const double cells = (double)r.p.Nx * r.p.Ny * got;
+      metrics << "{\"batch_steps\": " << got << ", \"wall_s\": " << wall
+              << ", \"cell_updates_per_s\": " << (wall > 0 ? cells / wall : 0.0) << "}\n";
+      metrics.flush();
+    }
     for (int k = 0; k < got; ++k) {
       const double *e = &rec[6 * k];
       if (!(k == 0 && resumed_after_save)) {  // that iteration's dt line preceded the save notice

@@ -64,13 +64,13 @@ def oracle_loop(o, p, t, ite, next_save):
     return snaps, lines, t
 
 
-def run_driver(tmp_path, name, restart=""):
+def run_driver(tmp_path, name, restart="", extra=()):
     from fv2d_gb300 import build as b
     b.build()
     exe = os.path.join(os.path.dirname(b.LIB), "..", "bin", "fv2d_gpu")
     ini = tmp_path / (name + ".ini.in")
     ini.write_text(INI.format(out=str(tmp_path), name=name, restart=restart))
-    r = subprocess.run([exe, str(ini)], cwd=str(tmp_path), capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe, str(ini), *extra], cwd=str(tmp_path), capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     return r.stdout
 
@@ -115,3 +115,30 @@ def test_driver_restart_matches_oracle(gpu_lib, tmp_path):
         rc, qg, tg, itg, err = read(L, f + ":/ite_%04d" % k, 64, 8)
         assert rc == 0, err
         assert tg == t and itg == k and bits_equal(qg, q), k
+
+
+def test_driver_metrics_log_is_the_iteration_log(gpu_lib, tmp_path):
+    """--metrics FILE: one JSON line per iteration (t, dt, inverse dt,
+    checkNegatives counts) equal to the oracle loop's, plus batch timings."""
+    import json
+    metrics = tmp_path / "m.jsonl"
+    run_driver(tmp_path, "run", extra=("--metrics", str(metrics)))
+    recs = [json.loads(line) for line in metrics.read_text().splitlines()]
+    steps = [r for r in recs if "step" in r]
+    batches = [r for r in recs if "batch_steps" in r]
+    p = reference_params(Nx=64, Ny=8, ymax=0.125, tend=0.05, save_freq=0.01, boundary_x=0, boundary_y=2,
+                         riemann_solver=1, reconstruction=2, CFL=0.8, gamma0=1.4, log_frequency=3)
+    o = Oracle(p)
+    o.init_problem("sod_x")
+    t = 0.0
+    ts, dts = [], []
+    while t + p.epsilon < p.tend:
+        d = o.compute_dt()
+        ts.append(t)
+        dts.append(d[0])
+        o.update(d[0])
+        t += d[0]
+    assert [r["step"] for r in steps] == list(range(len(dts)))
+    assert [r["t"] for r in steps] == ts and [r["dt"] for r in steps] == dts
+    assert all(r["neg_rho"] == 0 and r["neg_p"] == 0 and r["nan"] == 0 for r in steps)
+    assert sum(b["batch_steps"] for b in batches) == len(dts) and all(b["wall_s"] >= 0 for b in batches)
