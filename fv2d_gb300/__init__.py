@@ -59,6 +59,7 @@ def lib():
         L.fv2d_compute_dt.argtypes = [vp, _dp, _dp, _dp, _dp]
         L.fv2d_update.argtypes = [vp, C.c_double]
         L.fv2d_get_counters.argtypes = [vp, C.POINTER(C.c_uint64)]
+        L.fv2d_get_device_errors.argtypes = [vp, C.POINTER(C.c_int)]
         L.fv2d_advance.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_int, _dp,
                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.fv2d_get_time.argtypes = [vp, _dp, C.POINTER(C.c_int)]
@@ -222,6 +223,13 @@ class Simulation:
     def update(self, dt):
         """update(Q, U, dt) + consToPrim + checkNegatives (asynchronous)."""
         self._check(self._lib.fv2d_update(self.h, float(dt)))
+
+    def device_errors(self):
+        """Error bits set by this context's kernels (1 = a bounded wait gave
+        up, 2 = an index out of range in the bounds-check build)."""
+        v = C.c_int()
+        self._check(self._lib.fv2d_get_device_errors(self.h, C.byref(v)))
+        return v.value
 
     def counters(self):
         c = (C.c_uint64 * 3)()

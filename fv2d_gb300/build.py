@@ -1,6 +1,10 @@
 """Builds the native parts of fv2d_gb300 in-tree for GB300 (sm_103a):
 
   fv2d_gb300/lib/libfv2d_gpu.so   the C-ABI library (include/fv2d_gpu.h)
+  fv2d_gb300/bin/fv2d_gpu         the driver executable (main.cpp's role)
+  fv2d_gb300/lib_checked/...      build(bounds_check=True): the same library
+                                  with -DFV2D_BOUNDS_CHECK (index checks in
+                                  the FP64 step, for the tests)
 
 Translation units are compiled in parallel with nvcc (one -gencode,
 arch=compute_103a,code=sm_103a); object files go to fv2d_gb300/_build/.
@@ -72,9 +76,14 @@ def _compile(cmd):
     return r.stdout + r.stderr
 
 
-def build(verbose=False, jobs=None):
+def build(verbose=False, jobs=None, bounds_check=False):
     """Compile every translation unit and link libfv2d_gpu.so.  Returns the
-    library path."""
+    library path.  bounds_check=True builds the index-checking variant into
+    fv2d_gb300/lib_checked/ (objects in fv2d_gb300/_build_checked/)."""
+    BUILD = os.path.join(PKG, "_build_checked" if bounds_check else "_build")
+    LIBDIR = os.path.join(PKG, "lib_checked" if bounds_check else "lib")
+    LIB = os.path.join(LIBDIR, "libfv2d_gpu.so")
+    checked = ["-DFV2D_BOUNDS_CHECK"] if bounds_check else []
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     nvcc = _nvcc()
@@ -98,7 +107,7 @@ def build(verbose=False, jobs=None):
             continue
         if src.endswith(".cu"):
             cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                   *extra, "-c", s, "-o", o]
+                   *extra, *checked, "-c", s, "-o", o]
         else:
             cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-c", s, "-o", o]
         cmds.append(cmd)
@@ -109,6 +118,8 @@ def build(verbose=False, jobs=None):
                     print(out)
     if cmds or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         _compile([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fPIC"])
+    if bounds_check:
+        return LIB
     # the fv2d_gpu driver executable (main.cpp's role), linked to the library
     drv_src = os.path.join(PKG, "host", "driver.cpp")
     if not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < max(os.path.getmtime(LIB), os.path.getmtime(drv_src)):

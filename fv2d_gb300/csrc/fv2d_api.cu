@@ -637,6 +637,13 @@ int fv2d_update(fv2d_ctx *ctx, double dt) {
   return FV2D_OK;
 }
 
+int fv2d_get_device_errors(fv2d_ctx *ctx, int *bits) {
+  if (!ctx || !bits) return FV2D_ERR_INVALID;
+  if (int rc = sync_state(ctx)) return rc;
+  *bits = ctx->st_host->error;
+  return FV2D_OK;
+}
+
 int fv2d_get_counters(fv2d_ctx *ctx, uint64_t out[3]) {
   if (!ctx || !out) return FV2D_ERR_INVALID;
   if (int rc = sync_state(ctx)) return rc;

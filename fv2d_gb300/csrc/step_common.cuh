@@ -19,7 +19,7 @@ constexpr int NT = 288;            // threads per CTA (9 warps: the 544 faces of
 enum { RECON_PCM = 0, RECON_PLM = 2, RECON_MH = 3 };
 enum { STAGE_EULER = 0, STAGE_RK2_PREDICT = 1, STAGE_RK2_CORRECT = 2 };
 enum { RUN_RUNNING = 0, RUN_DONE = 1, RUN_SAVE = 2, RUN_NUMERIC = 3, RUN_PAUSED = 4 };
-enum { DEVERR_TMA_TIMEOUT = 1 };
+enum { DEVERR_TMA_TIMEOUT = 1, DEVERR_BOUNDS = 2 };
 
 // Simulation clock, dt and reduction accumulators, resident in device memory.
 // Written by the last CTA of each step (or by the set-up pass), read by the

@@ -91,6 +91,31 @@ __device__ __forceinline__ double warp_max_nonneg(double v) {
 }
 __device__ __forceinline__ unsigned warp_sum(unsigned v) { return __reduce_add_sync(0xffffffffu, v); }
 
+// Bounds-check build (-DFV2D_BOUNDS_CHECK, built for the tests as a stand-in
+// for a memory checker): every shared-memory index and every global plane
+// index of the step is checked; a bad one sets DEVERR_BOUNDS in the device
+// state and is redirected to a scratch slot (shared memory) or skipped
+// (global memory).  Without the macro the checks compile away.
+#ifdef FV2D_BOUNDS_CHECK
+constexpr bool kBoundsCheck = true;
+#else
+constexpr bool kBoundsCheck = false;
+#endif
+__device__ __forceinline__ int smem_index(int i, int total, int *err) {
+  if (kBoundsCheck && (i < 0 || i >= total)) {
+    atomicOr(err, DEVERR_BOUNDS);
+    return total;  // the spare slot past the layout
+  }
+  return i;
+}
+__device__ __forceinline__ bool gidx_ok(long long i, long long n, int *err) {
+  if (kBoundsCheck && (i < 0 || i >= n)) {
+    atomicOr(err, DEVERR_BOUNDS);
+    return false;
+  }
+  return true;
+}
+
 // Shared-memory layout (in doubles) for a reconstruction type, with or
 // without the viscous face terms.
 template <int RECON, bool VISC = false>
@@ -108,7 +133,7 @@ struct Smem {
   static constexpr int VX = T + R1;                                  // viscous x-face terms, 3 x TY x (TX+1)
   static constexpr int VY = VX + (VISC ? 3 * TY * (TX + 1) : 0);     // viscous y-face terms, 3 x (TY+1) x TX
   static constexpr int TOTAL = VY + (VISC ? 3 * (TY + 1) * TX : 0);
-  static constexpr size_t BYTES = sizeof(double) * TOTAL + 128;  // + alignment slack
+  static constexpr size_t BYTES = sizeof(double) * (TOTAL + 1) + 128;  // + spare slot + alignment slack
 };
 
 template <int RECON, int RS, bool VISC>
@@ -149,9 +174,11 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
   }
   mbar_wait_bounded(&mbar, &st->error);
 
-  auto sQ = [&](int k, int ly, int lx) -> double & { return sm[L::Q + (k * SH + ly) * SW + lx]; };
+  auto SMI = [&](int i) -> double & { return sm[smem_index(i, L::TOTAL, &st->error)]; };
+  auto gok = [&](long long i, long long n) { return gidx_ok(i, n, &st->error); };
+  auto sQ = [&](int k, int ly, int lx) -> double & { return SMI(L::Q + (k * SH + ly) * SW + lx); };
   auto sR1 = [&](int base, int k, int ly, int lx) -> double & {
-    return sm[base + (k * L::R1H + (ly - 1)) * L::R1W + (lx - 1)];
+    return SMI(base + (k * L::R1H + (ly - 1)) * L::R1W + (lx - 1));
   };
   auto cellQ = [&](int ly, int lx) -> S4<double> {
     return S4<double>{sQ(0, ly, lx), sQ(1, ly, lx), sQ(2, ly, lx), sQ(3, ly, lx)};
@@ -166,17 +193,17 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     // DY[k][g][c] = Q(g+1) - Q(g) on padded column c+2.
     constexpr int NDX = 4 * TY * (TX + 3), NDY = 4 * (TY + 3) * TX;
     static_assert(NDX + NDY <= L::T - L::FX, "difference arrays exceed the face-flux area");
-    double *DX = sm + L::FX, *DY = sm + L::FX + NDX;
+    // DX at L::FX, DY at L::FX + NDX
     for (int it = tid; it < NDX + NDY; it += NT) {
       if (it < NDX) {
         const int k = it / (TY * (TX + 3)), rem = it % (TY * (TX + 3));
         const int ly = rem / (TX + 3) + 2, lx = rem % (TX + 3) + 1;
-        DX[it] = sQ(k, ly, lx) - sQ(k, ly, lx - 1);
+        SMI(L::FX + it) = sQ(k, ly, lx) - sQ(k, ly, lx - 1);
       } else {
         const int jt = it - NDX;
         const int k = jt / ((TY + 3) * TX), rem = jt % ((TY + 3) * TX);
         const int ly = rem / TX + 1, lx = rem % TX + 2;
-        DY[jt] = sQ(k, ly, lx) - sQ(k, ly - 1, lx);
+        SMI(L::FX + NDX + jt) = sQ(k, ly, lx) - sQ(k, ly - 1, lx);
       }
     }
     __syncthreads();
@@ -188,16 +215,16 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         const int r = it / (TX + 2), c = it % (TX + 2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const double *d = DX + (k * TY + r) * (TX + 3) + c;  // d[0] = dL, d[1] = dR of column c+1
-          sR1(L::SX, k, r + 2, c + 1) = fv_half(minmod(d[0], d[1]));
+          const int d = L::FX + (k * TY + r) * (TX + 3) + c;  // dL, dR of column c+1
+          sR1(L::SX, k, r + 2, c + 1) = fv_half(minmod(SMI(d), SMI(d + 1)));
         }
       } else {
         const int jt = it - NXS;
         const int g = jt / TX, c = jt % TX;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const double *d = DY + (k * (TY + 3) + g) * TX + c;  // d[0] = dU, d[TX] = dD of row g+1
-          sR1(L::SY, k, g + 1, c + 2) = fv_half(minmod(d[0], d[TX]));
+          const int d = L::FX + NDX + (k * (TY + 3) + g) * TX + c;  // dU, dD of row g+1
+          sR1(L::SY, k, g + 1, c + 2) = fv_half(minmod(SMI(d), SMI(d + TX)));
         }
       }
     }
@@ -285,18 +312,18 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
       double pout;
       riemann<RS>(qL, qR, fl, pout, ydir ? a.gy_dy : a.gx_dx, gas);
       if (!ydir) {
-        double *F = sm + L::FX + r * (TX + 1) + c;
-        F[0] = fl.r;
-        F[1 * TY * (TX + 1)] = fl.u;
-        F[2 * TY * (TX + 1)] = fl.v;
-        F[3 * TY * (TX + 1)] = fl.p;
+        const int F = L::FX + r * (TX + 1) + c;
+        SMI(F) = fl.r;
+        SMI(F + 1 * TY * (TX + 1)) = fl.u;
+        SMI(F + 2 * TY * (TX + 1)) = fl.v;
+        SMI(F + 3 * TY * (TX + 1)) = fl.p;
       } else {
-        double *F = sm + L::FY + r * TX + c;
-        F[0] = fl.r;
-        F[1 * (TY + 1) * TX] = fl.v;  // swap back (Update.h:145-146)
-        F[2 * (TY + 1) * TX] = fl.u;
-        F[3 * (TY + 1) * TX] = fl.p;
-        sm[L::PY + r * TX + c] = pout;
+        const int F = L::FY + r * TX + c;
+        SMI(F) = fl.r;
+        SMI(F + 1 * (TY + 1) * TX) = fl.v;  // swap back (Update.h:145-146)
+        SMI(F + 2 * (TY + 1) * TX) = fl.u;
+        SMI(F + 3 * (TY + 1) * TX) = fl.p;
+        SMI(L::PY + r * TX + c) = pout;
       }
     }
   }
@@ -323,10 +350,9 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         const double dvdy = 0.25 * ody * (V_(1, xs) - V_(-1, xs) + V_(1, xm) - V_(-1, xm));
         const double tau_xx = four_thirds * dudx - two_thirds * dvdy;
         const double tau_xy = dvdx + dudy;
-        double *Vf = sm + L::VX + f;
-        Vf[0] = mu * tau_xx;
-        Vf[NVX] = mu * tau_xy;
-        Vf[2 * NVX] = mu * (tau_xx * qiu + tau_xy * qiv);
+        SMI(L::VX + f) = mu * tau_xx;
+        SMI(L::VX + f + NVX) = mu * tau_xy;
+        SMI(L::VX + f + 2 * NVX) = mu * (tau_xx * qiu + tau_xy * qiv);
       } else {  // between rows r+1 (s-1) and r+2 (s) of column c+2
         const int g = f - NVX;
         const int r = g / TX, c = g % TX;
@@ -341,10 +367,9 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         const double dvdx = 0.25 * odx * (V_(ys, 1) - V_(ys, -1) + V_(ym, 1) - V_(ym, -1));
         const double tau_yy = four_thirds * dvdy - two_thirds * dudx;
         const double tau_xy = dvdx + dudy;
-        double *Vf = sm + L::VY + g;
-        Vf[0] = mu * tau_xy;
-        Vf[NVY] = mu * tau_yy;
-        Vf[2 * NVY] = mu * (tau_xy * qiu + tau_yy * qiv);
+        SMI(L::VY + g) = mu * tau_xy;
+        SMI(L::VY + g + NVY) = mu * tau_yy;
+        SMI(L::VY + g + 2 * NVY) = mu * (tau_xy * qiu + tau_yy * qiv);
       }
     }
   }
@@ -367,6 +392,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     if (i >= a.Nx || j >= a.Ny) continue;
     const int ly = ry + 2, lx = rx + 2;
     const long long g = (long long)(j + HALO) * P + (i + HALO);
+    if (!gok(g, PL)) continue;
     double un[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) un[k] = Usrc[k * PL + g];
@@ -374,11 +400,12 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
 
     // x direction (Update.h:114-168 with dir = IX)
     {
-      const double *F = sm + L::FX + ry * (TX + 1) + rx;
+      const int F = L::FX + ry * (TX + 1) + rx;
       constexpr int S = TY * (TX + 1);
-      const double FL0 = F[0], FR0 = F[1];
+      const double FL0 = SMI(F), FR0 = SMI(F + 1);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) un[k] += ddivc(mulx<3>(F[k * S] - F[k * S + 1], dt), a.dx, a.inv_dx, a.dx_pow2);
+      for (int k = 0; k < 4; ++k)
+        un[k] += ddivc(mulx<3>(SMI(F + k * S) - SMI(F + k * S + 1), dt), a.dx, a.inv_dx, a.dx_pow2);
       if (a.grav_mode) {
         const double gv = (a.grav_mode == 1) ? a.gxf : (double)a.grav_row[j];
         un[2] += dt * rho * gv;
@@ -387,23 +414,23 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     }
     // y direction (dir = IY), with the well-balanced boundary override
     {
-      const double *F = sm + L::FY + ry * TX + rx;
+      const int F = L::FY + ry * TX + rx;
       constexpr int S = (TY + 1) * TX;
       double FL[4], FR[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        FL[k] = F[k * S];
-        FR[k] = F[k * S + TX];
+        FL[k] = SMI(F + k * S);
+        FR[k] = SMI(F + k * S + TX);
       }
       double gv = 0.0;
       if (a.grav_mode) gv = (a.grav_mode == 1) ? a.gyf : (double)a.grav_row[j];
       if (a.wb && (j == 0 || j == a.Ny - 1)) {  // Update.h:149-156
         const double gy = (a.grav_mode == 0) ? 0.0 : gv;
         if (j == 0) {
-          const double poutR = sm[L::PY + (ry + 1) * TX + rx];
+          const double poutR = SMI(L::PY + (ry + 1) * TX + rx);
           FL[0] = 0.0; FL[1] = 0.0; FL[2] = poutR - rho * gy * a.dy; FL[3] = 0.0;
         } else {
-          const double poutL = sm[L::PY + ry * TX + rx];
+          const double poutL = SMI(L::PY + ry * TX + rx);
           FR[0] = 0.0; FR[1] = 0.0; FR[2] = poutL + rho * gy * a.dy; FR[3] = 0.0;
         }
       }
@@ -443,21 +470,21 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     // -side face negated, accumulated in the reference's order
     if constexpr (VISC) {
       constexpr int NVX = TY * (TX + 1), NVY = (TY + 1) * TX;
-      const double *Vw = sm + L::VX + ry * (TX + 1) + rx;  // x face at rx (west), rx + 1 (east)
-      const double *Vn = sm + L::VY + ry * TX + rx;        // y face at ry (north), ry + 1 (south)
+      const int Vw = L::VX + ry * (TX + 1) + rx;  // x face at rx (west), rx + 1 (east)
+      const int Vn = L::VY + ry * TX + rx;        // y face at ry (north), ry + 1 (south)
       double fx1 = 0.0, fx2 = 0.0, fx3 = 0.0, fy1 = 0.0, fy2 = 0.0, fy3 = 0.0;
-      fx1 += -Vw[0];
-      fx2 += -Vw[NVX];
-      fx3 += -Vw[2 * NVX];
-      fy1 += -Vn[0];
-      fy2 += -Vn[NVY];
-      fy3 += -Vn[2 * NVY];
-      fx1 += Vw[1];
-      fx2 += Vw[NVX + 1];
-      fx3 += Vw[2 * NVX + 1];
-      fy1 += Vn[TX];
-      fy2 += Vn[NVY + TX];
-      fy3 += Vn[2 * NVY + TX];
+      fx1 += -SMI(Vw);
+      fx2 += -SMI(Vw + NVX);
+      fx3 += -SMI(Vw + 2 * NVX);
+      fy1 += -SMI(Vn);
+      fy2 += -SMI(Vn + NVY);
+      fy3 += -SMI(Vn + 2 * NVY);
+      fx1 += SMI(Vw + 1);
+      fx2 += SMI(Vw + NVX + 1);
+      fx3 += SMI(Vw + 2 * NVX + 1);
+      fy1 += SMI(Vn + TX);
+      fy2 += SMI(Vn + NVY + TX);
+      fy3 += SMI(Vn + 2 * NVY + TX);
       un[0] += (0.0 + 0.0) * dt;
       un[1] += (fx1 + fy1) * dt;
       un[2] += (fx2 + fy2) * dt;
@@ -487,7 +514,8 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
     Qd[PL + g] = q.u;
     Qd[2 * PL + g] = q.v;
     Qd[3 * PL + g] = q.p;
-    if (final_stage && a.mirror) {  // interleaved interior copy in host memory (over the C2C link)
+    if (final_stage && a.mirror && gok((long long)j * a.Nx + i, (long long)a.Nx * a.Ny)) {
+      // interleaved interior copy in host memory (over the C2C link)
       double2 *m = reinterpret_cast<double2 *>(a.mirror + ((long long)j * a.Nx + i) * 4);
       m[0] = make_double2(q.r, q.u);
       m[1] = make_double2(q.v, q.p);
@@ -505,6 +533,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
         for (int c = 0; c < cx; ++c) {
           if (b == 0 && c == 0) continue;
           const long long gg = (long long)(ty[b] + HALO) * P + (tx[c] + HALO);
+          if (!gok(gg, PL)) continue;
           Qd[gg] = q.r;
           Qd[PL + gg] = nx[c] ? q.u * -1.0 : q.u;
           Qd[2 * PL + gg] = ny[b] ? q.v * -1.0 : q.v;

@@ -100,6 +100,11 @@ int fv2d_update(fv2d_ctx *ctx, double dt);
  * checkNegatives of the last update.  Synchronises. */
 int fv2d_get_counters(fv2d_ctx *ctx, uint64_t out[3]);
 
+/* Error bits set by the context's kernels since it was created (no reference
+ * counterpart): 1 = a bounded TMA wait gave up, 2 = an index out of range
+ * (only the bounds-check build, -DFV2D_BOUNDS_CHECK, tests for these). */
+int fv2d_get_device_errors(fv2d_ctx *ctx, int *bits);
+
 /* Device-driven main loop.  Runs at most max_steps iterations of
  *   while (t + epsilon < tend) { [stop if t + epsilon > next_save];
  *                                dt = computeDt; update; t += dt; }
