@@ -52,6 +52,22 @@ def workload_params(fv, n):
                              boundary_y=fv.BC_REFLECTING, time_stepping=fv.TS_EULER)
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """Maximum of x over the ranks of the default process group (x itself
+    when there is none): the slowest replica sets the whole job's time."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds_max):
+    """Units processed by all replicas per second of the slowest one."""
+    return world * units_per_rank / seconds_max
+
+
 def config(n, steps):
     return {"workload": WORKLOAD, "grid": [n, n], "problem": "sedov", "scheme": "PLM-minmod + HLLC, Euler",
             "cfl": 0.8, "gamma": 1.4, "boundaries": "reflecting", "steps": steps,
@@ -381,13 +397,9 @@ def main():
     t_sim, ite = sim.time()
     if ite != args.steps:
         raise RuntimeError(f"expected {args.steps} iterations, device reports {ite}")
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, dist, "cuda")
     cells = NX * NY
-    value = world * cells * args.steps / (ms_max * 1e-3)
+    value = whole_job_rate(cells * args.steps, world, ms_max * 1e-3)
     ms_step = ms_max / args.steps
 
     # roofline of the fused step kernel (one step launch + a one-thread commit per iteration)
@@ -426,12 +438,8 @@ def main():
         sim.update(sim.compute_dt()[0])
         sim.get_prim_ptr(q1.data_ptr())
     el = time.perf_counter() - t0
-    el_max = el
-    if dist is not None:
-        t = torch.tensor([el], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el_max = float(t.item())
-    e2e = {"value": world * cells * ke / el_max, "unit": METRIC, "h2d_bytes_per_step": cells * 32,
+    el_max = max_over_ranks(el, dist, "cuda")
+    e2e = {"value": whole_job_rate(cells * ke, world, el_max), "unit": METRIC, "h2d_bytes_per_step": cells * 32,
            "d2h_bytes_per_step": cells * 32 + 8, "steps": ke,
            "path": "fv2d_set_prim(pinned host, read by the set-up kernel) + fv2d_compute_dt + fv2d_update "
                    "(writes the pinned host mirror while it computes) + fv2d_get_prim(mirror: waits for the step)"}
