@@ -509,7 +509,11 @@ def main():
         "config": config(NX, args.steps),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": (traffic * cells) if traffic else None, "peak_kind": peak_kind,
-                     "bytes_per_cell": BYTES_PER_CELL, "kernel": "fv2d::step_kernel<PLM,HLLC>"},
+                     "bytes_per_cell": BYTES_PER_CELL, "kernel": "fv2d::step_kernel<PLM,HLLC>",
+                     "duration": "CUDA events per iteration: the step kernel plus its one-thread commit kernel "
+                                 "(~4.6 us, 0.3 % of the iteration in the ncu launch list)",
+                     "binding": "instruction issue, not HBM: binary64 pipe ~65 %, integer ALU ~48 % busy "
+                                "(profiles/step_fp64_plm_hllc_sedov.txt); see roofline_fp64"},
         "roofline_fp64": fp64,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": 2 * args.steps + 1,  # begin_kernel, then step_kernel + commit_kernel per iteration
