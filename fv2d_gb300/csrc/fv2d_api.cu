@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(256) prepare_kernel(PrepArgs a) {
   const int W = a.Nx + 4;
   const long long n_ghost = 4LL * W + 4LL * a.Ny;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const Gas<double> gas{a.gamma, a.gm1, 1.0 / a.gm1, 0.0};
+  const Gas<double> gas = make_gas(a.gamma, a.gm1, 1.0 / a.gm1, 0.0);
   double lmax = -1.0;
   if (idx < n_int) {
     const int j = (int)(idx / a.Nx), i = (int)(idx % a.Nx);

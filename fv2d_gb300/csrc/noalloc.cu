@@ -66,7 +66,7 @@ __device__ __forceinline__ double div_spacing(double x, double d, double inv_d, 
 __global__ void __launch_bounds__(kThreads) dt_noalloc_kernel(DtArgs a) {
   __shared__ double red[kThreads / 32];
   __shared__ int s_last;
-  const fv2d::Gas<double> gas{a.gamma, a.gm1, 1.0 / a.gm1, 0.0};
+  const fv2d::Gas<double> gas = fv2d::make_gas(a.gamma, a.gm1, 1.0 / a.gm1, 0.0);
   double m = -1.0;
   const long long base = (long long)blockIdx.x * kCellsPerBlock;
 #pragma unroll

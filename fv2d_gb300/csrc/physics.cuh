@@ -55,6 +55,25 @@ __host__ __device__ __forceinline__ double fv_sqrt(double x) {
 #endif
 }
 __host__ __device__ __forceinline__ float fv_sqrt(float x) { return sqrtf(x); }
+// Several quotients by one divisor: r = fv_recip(b) once, fv_div_by(a, b, r)
+// per dividend (binary64 on the device: the reciprocal word of b is formed
+// once; the quotients are the same correctly rounded values as a / b).
+__host__ __device__ __forceinline__ uint64_t fv_recip(double b) {
+#ifdef __CUDA_ARCH__
+  return softfp::recip_of(b);
+#else
+  return 0ull;
+#endif
+}
+__host__ __device__ __forceinline__ double fv_div_by(double a, double b, uint64_t r) {
+#ifdef __CUDA_ARCH__
+  return softfp::div_by(a, b, r);
+#else
+  return a / b;
+#endif
+}
+__host__ __device__ __forceinline__ uint64_t fv_recip(float) { return 0ull; }
+__host__ __device__ __forceinline__ float fv_div_by(float a, float b, uint64_t) { return a / b; }
 
 // Comparisons, fmin / fmax and scalings by 1/2: on the device, binary64 goes
 // through the bit-pattern forms of softfp.cuh (IEEE results, integer pipe).
@@ -119,7 +138,13 @@ struct Gas {
   R gm1;     // gamma0 - 1.0
   R entho;   // 1.0 / (gamma0 - 1.0)               (RiemannSolvers.h:76)
   R fslp_K;  // FSLP K                              (SimInfo.h:399)
+  uint64_t rgm1;  // fv_recip(gm1): the divisions by gamma0 - 1 (set by make_gas)
 };
+
+template <class R>
+__host__ __device__ __forceinline__ Gas<R> make_gas(R gamma, R gm1, R entho, R fslp_K) {
+  return Gas<R>{gamma, gm1, entho, fslp_K, fv_recip(gm1)};
+}
 
 // States.h:19-30
 template <class R>
@@ -129,7 +154,7 @@ __host__ __device__ __forceinline__ S4<R> prim_to_cons(const S4<R> &q, const Gas
   s.u = q.r * q.u;
   s.v = q.r * q.v;
   R Ek = fv_div(fv_half(s.u * s.u + s.v * s.v), q.r);
-  s.p = (Ek + fv_div(q.p, g.gm1));
+  s.p = (Ek + fv_div_by(q.p, g.gm1, g.rgm1));
   return s;
 }
 
@@ -154,6 +179,11 @@ template <class R>
 __device__ __forceinline__ R sound_speed(const S4<R> &q, const Gas<R> &g) {
   return dsqrt(fv_div(mulx<1>(q.p, g.gamma), q.r));
 }
+// the same with the reciprocal of q.r already formed (fv_recip)
+template <class R>
+__device__ __forceinline__ R sound_speed_r(const S4<R> &q, const Gas<R> &g, uint64_t rr) {
+  return dsqrt(fv_div_by(mulx<1>(q.p, g.gamma), q.r, rr));
+}
 
 // Update.h:77-85
 template <class R>
@@ -171,8 +201,10 @@ __device__ __forceinline__ R sel(bool c, R a, R b) {
 // in the reference's branch order (SL >= 0, SR <= 0, else the HLL state).
 template <class R>
 __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4<R> &f, R &pout, const Gas<R> &g) {
-  const R aL = sound_speed(qL, g);
-  const R aR = sound_speed(qR, g);
+  // every quotient by rho_L (rho_R) shares one reciprocal
+  const uint64_t rL = fv_recip(qL.r), rR = fv_recip(qR.r);
+  const R aL = sound_speed_r(qL, g, rL);
+  const R aR = sound_speed_r(qR, g, rR);
   const R sminL = qL.u - aL;
   const R smaxL = qL.u + aL;
   const R sminR = qR.u - aR;
@@ -181,8 +213,8 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   const R SR = fv_fmax(smaxL, smaxR);
   // computeFlux (RiemannSolvers.h:133-141).  p/(gamma-1) is also the pressure
   // term of primToCons below: the same division, evaluated once.
-  const R peL = fv_div(qL.p, g.gm1);
-  const R peR = fv_div(qR.p, g.gm1);
+  const R peL = fv_div_by(qL.p, g.gm1, g.rgm1);
+  const R peR = fv_div_by(qR.p, g.gm1, g.rgm1);
   const R EkL = fv_half(qL.r) * (qL.u * qL.u + qL.v * qL.v);
   const R EkR = fv_half(qR.r) * (qR.u * qR.u + qR.v * qR.v);
   const R EL = (peL + EkL);
@@ -192,15 +224,16 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   S4<R> FR{ruR, ruR * qR.u + qR.p, ruR * qR.v, (qR.p + ER) * qR.u};
   // primToCons (States.h:19-30) of both states
   const R mvL = qL.r * qL.v, mvR = qR.r * qR.v;
-  const R uEL = (fv_div(fv_half(ruL * ruL + mvL * mvL), qL.r) + peL);
-  const R uER = (fv_div(fv_half(ruR * ruR + mvR * mvR), qR.r) + peR);
+  const R uEL = (fv_div_by(fv_half(ruL * ruL + mvL * mvL), qL.r, rL) + peL);
+  const R uER = (fv_div_by(fv_half(ruR * ruR + mvR * mvR), qR.r, rR) + peR);
   const R SLSR = SL * SR;
   const R den = SR - SL;
+  const uint64_t rden = fv_recip(den);
   S4<R> FM;
-  fv_div2(SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r), SR * FL.u - SL * FR.u + SLSR * (ruR - ruL), den, FM.r,
-          FM.u);
-  fv_div2(SR * FL.v - SL * FR.v + SLSR * (mvR - mvL), SR * FL.p - SL * FR.p + SLSR * (uER - uEL), den, FM.v,
-          FM.p);
+  FM.r = fv_div_by(SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r), den, rden);
+  FM.u = fv_div_by(SR * FL.u - SL * FR.u + SLSR * (ruR - ruL), den, rden);
+  FM.v = fv_div_by(SR * FL.v - SL * FR.v + SLSR * (mvR - mvL), den, rden);
+  FM.p = fv_div_by(SR * FL.p - SL * FR.p + SLSR * (uER - uEL), den, rden);
   const R pM = fv_half(qL.p + qR.p);
   const bool left = fv_ge0(SL);
   const bool right = !left && fv_le0(SR);
@@ -279,7 +312,7 @@ __device__ __forceinline__ void riemann_fslp(const S4<R> &qL, const S4<R> &qR, S
   const R sv = up ? qL.v : qR.v;
   const R sp = up ? qL.p : qR.p;
   const R Ekstar = fv_half(sr) * (su * su + sv * sv);
-  const R Estar = Ekstar + fv_div(sp, g.gm1);
+  const R Estar = Ekstar + fv_div_by(sp, g.gm1, g.rgm1);
   f.r = ustar * sr;
   f.u = ustar * sr * su + Pi;
   f.v = ustar * sr * sv;

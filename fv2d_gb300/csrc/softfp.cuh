@@ -169,6 +169,22 @@ static __device__ __noinline__ double2 div2_rn(double a1, double a2, double b) {
   return make_double2(div_finish(o1, a1, b, v), div_finish(o2, a2, b, v));
 }
 
+// Quotients by one divisor b: recip_of(b) computes its reciprocal word once
+// (0 when b is zero, subnormal, infinite or NaN: the hardware handles every
+// quotient by such a b), div_by(a, b, v) forms each quotient.
+static __device__ __noinline__ uint64_t recip_of(double b) {
+  const uint64_t ib = bits(b);
+  const int eb = (int)((ib >> 52) & 0x7ff);
+  if (eb == 0 || eb == 0x7ff) return 0ull;
+  return recip_word(((ib & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11);
+}
+static __device__ __noinline__ double div_by(double a, double b, uint64_t v) {
+  const DivOp o = div_begin(a, b);
+  // a normal divisor's reciprocal word is never 0 (it is at least 2^11)
+  if (o.fast && v == 0ull) return div_rn(a, b);
+  return div_finish(o, a, b, v);
+}
+
 // sqrt(x), round to nearest even.
 static __device__ __noinline__ double sqrt_rn(double x) {
   const uint64_t ix = bits(x);

@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
   auto cellQ = [&](int ly, int lx) -> S4<double> {
     return S4<double>{sQ(0, ly, lx), sQ(1, ly, lx), sQ(2, ly, lx), sQ(3, ly, lx)};
   };
-  const Gas<double> gas{a.gamma, a.gm1, a.entho, a.fslp_K};
+  const Gas<double> gas = make_gas(a.gamma, a.gm1, a.entho, a.fslp_K);
 
   // ---- 2. slopes (+ MUSCL-Hancock predictor) and temperatures ------------
   if constexpr (RECON == RECON_PLM) {
