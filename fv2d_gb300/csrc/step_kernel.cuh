@@ -137,7 +137,7 @@ struct Smem {
 };
 
 template <int RECON, int RS, bool VISC>
-__global__ void __launch_bounds__(NT, (RECON == RECON_MH) ? 1 : 3)
+__global__ void __launch_bounds__(NT, 3)
     step_kernel(const __grid_constant__ CUtensorMap tmQ0, const __grid_constant__ CUtensorMap tmQ1,
                 const StepArgs a) {
   using L = Smem<RECON, VISC>;
