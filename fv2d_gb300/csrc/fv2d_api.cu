@@ -100,8 +100,8 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 }
 
 // ------------------------------------------------------------------ kernels
-__device__ __forceinline__ double ddiv_c(double x, double d, double inv_d, int pow2) {
-  return pow2 ? x * inv_d : fv_div(x, d);
+__device__ __forceinline__ double ddiv_c(double x, double d, double inv_d, int pow2, uint64_t rw) {
+  return pow2 ? x * inv_d : fv_div_by(x, d, rw);
 }
 
 // Set-up pass: interleaved interior primitives -> planes, every ghost cell
@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(256) prepare_kernel(PrepArgs a) {
     a.U[2 * a.plane + g] = u.v;
     a.U[3 * a.plane + g] = u.p;
     const double cs = sound_speed(q, gas);
-    const double ih = ddiv_c(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2) + ddiv_c(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2);
+    const double ih = ddiv_c(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx) +
+                      ddiv_c(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
     lmax = fmax(lmax, ih);
   } else if (idx < n_int + n_ghost) {
     long long k = idx - n_int;
@@ -258,6 +259,8 @@ void fill_args(fv2d_ctx *c) {
   a.dy_pow2 = is_pow2_spacing(a.dy);
   a.inv_dx = a.dx_pow2 ? 1.0 / a.dx : 0.0;
   a.inv_dy = a.dy_pow2 ? 1.0 / a.dy : 0.0;
+  a.rw_dx = softfp::recip_of_host(a.dx);
+  a.rw_dy = softfp::recip_of_host(a.dy);
   a.one_over_dx = 1.0 / a.dx;
   a.one_over_dy = 1.0 / a.dy;
   a.gx_dx = p.gx * a.dx;
@@ -344,6 +347,8 @@ int run_prepare(fv2d_ctx *ctx, const double *src) {
   pa.inv_dy = ctx->args.inv_dy;
   pa.dx_pow2 = ctx->args.dx_pow2;
   pa.dy_pow2 = ctx->args.dy_pow2;
+  pa.rw_dx = ctx->args.rw_dx;
+  pa.rw_dy = ctx->args.rw_dy;
   pa.CFL = p.CFL;
   pa.inv_tc = ctx->inv_tc;
   pa.inv_visc = ctx->inv_visc;

@@ -53,11 +53,12 @@ struct DtArgs {
   int nblocks;
   double gamma, gm1, dx, dy, inv_dx, inv_dy;
   int dx_pow2, dy_pow2;
+  uint64_t rw_dx, rw_dy;  // reciprocal words of dx, dy (quotients when 1/dx is inexact)
   double CFL, inv_tc, inv_visc;
 };
 
-__device__ __forceinline__ double div_spacing(double x, double d, double inv_d, int pow2) {
-  return pow2 ? x * inv_d : fv2d::fv_div(x, d);
+__device__ __forceinline__ double div_spacing(double x, double d, double inv_d, int pow2, uint64_t rw) {
+  return pow2 ? x * inv_d : fv2d::fv_div_by(x, d, rw);
 }
 
 // Same per-cell expression and the same max semantics as the dt reduction of
@@ -76,8 +77,8 @@ __global__ void __launch_bounds__(kThreads) dt_noalloc_kernel(DtArgs a) {
       const double *s = a.q + c * 4;
       const fv2d::S4<double> q{s[0], s[1], s[2], s[3]};
       const double cs = fv2d::sound_speed(q, gas);
-      const double ih = div_spacing(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2) +
-                        div_spacing(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2);
+      const double ih = div_spacing(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx) +
+                        div_spacing(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
       m = fmax(m, ih);
     }
   }
@@ -171,6 +172,8 @@ extern "C" int fv2d_compute_dt_noalloc(const fv2d_params *p, const double *q_dev
   a.dy_pow2 = pow2_spacing(a.dy);
   a.inv_dx = a.dx_pow2 ? 1.0 / a.dx : 0.0;
   a.inv_dy = a.dy_pow2 ? 1.0 / a.dy : 0.0;
+  a.rw_dx = fv2d::softfp::recip_of_host(a.dx);
+  a.rw_dy = fv2d::softfp::recip_of_host(a.dy);
   a.CFL = p->CFL;
   fv2d::parabolic_inv_dt(*p, &a.inv_tc, &a.inv_visc);
   dt_noalloc_kernel<<<a.nblocks, kThreads, 0, s>>>(a);

@@ -185,6 +185,21 @@ static __device__ __noinline__ double div_by(double a, double b, uint64_t v) {
   return div_finish(o, a, b, v);
 }
 
+// recip_of(b) for a divisor known on the host (the mesh spacings): the same
+// word from its definition, floor((2^128 - 1) / d) - 2^64 with d the
+// divisor's significand aligned to bit 63; the quotient lies in
+// [2^64, 2^65), so its low 64 bits are the word.
+inline uint64_t recip_of_host(double b) {
+  union {
+    double f;
+    uint64_t u;
+  } c{b};
+  const int eb = (int)((c.u >> 52) & 0x7ff);
+  if (eb == 0 || eb == 0x7ff) return 0ull;
+  const uint64_t d = ((c.u & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11;
+  return (uint64_t)(~(unsigned __int128)0 / d);
+}
+
 // sqrt(x), round to nearest even.
 static __device__ __noinline__ double sqrt_rn(double x) {
   const uint64_t ix = bits(x);

@@ -65,6 +65,7 @@ struct StepArgs {
   double gamma, gm1, entho, fslp_K;
   double dx, dy, inv_dx, inv_dy;
   int dx_pow2, dy_pow2;  // 1/dx (1/dy) is exact: divisions become products
+  uint64_t rw_dx, rw_dy;  // otherwise quotients by dx (dy) share its reciprocal word
   double one_over_dx, one_over_dy;  // 1.0/dx, 1.0/dy (Viscosity.h:168-169)
   double gx_dx, gy_dy;  // FSLP gravity terms gx*dx, gy*dy (Update.h:119)
   double gxf, gyf;      // constant gravity narrowed to float (Gravity.h:39)
@@ -90,6 +91,7 @@ struct PrepArgs {
   int pitch, Nx, Ny, nblocks;
   double gamma, gm1, dx, dy, inv_dx, inv_dy;
   int dx_pow2, dy_pow2;
+  uint64_t rw_dx, rw_dy;
   double CFL, inv_tc, inv_visc;
   int bcx, bcy;
 };

@@ -77,11 +77,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err_flag, 
   return false;
 }
 
-__device__ __forceinline__ double ddivc(double x, double d, double inv_d, int pow2) {
+__device__ __forceinline__ double ddivc(double x, double d, double inv_d, int pow2, uint64_t rw) {
   // x / d; when 1/d is exactly representable the product is the same
-  // correctly rounded value.
+  // correctly rounded value; otherwise the quotient uses d's reciprocal word
+  // rw, formed once on the host.
   if (pow2) return softfp::mul_pow2(x, inv_d, (int)((softfp::bits(inv_d) >> 52) & 0x7FF) - 1023);
-  return fv_div(x, d);
+  return fv_div_by(x, d, rw);
 }
 
 __device__ __forceinline__ double warp_max_nonneg(double v) {
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(NT, 3)
       const double FL0 = SMI(F), FR0 = SMI(F + 1);
 #pragma unroll
       for (int k = 0; k < 4; ++k)
-        un[k] += ddivc(mulx<3>(SMI(F + k * S) - SMI(F + k * S + 1), dt), a.dx, a.inv_dx, a.dx_pow2);
+        un[k] += ddivc(mulx<3>(SMI(F + k * S) - SMI(F + k * S + 1), dt), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx);
       if (a.grav_mode) {
         const double gv = (a.grav_mode == 1) ? a.gxf : (double)a.grav_row[j];
         un[2] += dt * rho * gv;
@@ -435,7 +436,7 @@ __global__ void __launch_bounds__(NT, 3)
         }
       }
 #pragma unroll
-      for (int k = 0; k < 4; ++k) un[k] += ddivc(mulx<3>(FL[k] - FR[k], dt), a.dy, a.inv_dy, a.dy_pow2);
+      for (int k = 0; k < 4; ++k) un[k] += ddivc(mulx<3>(FL[k] - FR[k], dt), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
       if (a.grav_mode) {
         un[2] += dt * rho * gv;
         un[3] += dt * 0.5 * (FL[0] + FR[0]) * gv;
@@ -448,19 +449,19 @@ __global__ void __launch_bounds__(NT, 3)
       const double TU = sR1(L::T, 0, ly - 1, lx), TD = sR1(L::T, 0, ly + 1, lx);
       const double kL = a.kap_row[4 * j + 0], kR = a.kap_row[4 * j + 1];
       const double kU = a.kap_row[4 * j + 2], kD = a.kap_row[4 * j + 3];
-      double FLt = ddivc(kL * (TC - TL), a.dx, a.inv_dx, a.dx_pow2);
-      double FRt = ddivc(kR * (TR - TC), a.dx, a.inv_dx, a.dx_pow2);
-      const double FUt = ddivc(kU * (TC - TU), a.dy, a.inv_dy, a.dy_pow2);
-      const double FDt = ddivc(kD * (TD - TC), a.dy, a.inv_dy, a.dy_pow2);
+      double FLt = ddivc(kL * (TC - TL), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx);
+      double FRt = ddivc(kR * (TR - TC), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx);
+      const double FUt = ddivc(kU * (TC - TU), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
+      const double FDt = ddivc(kD * (TD - TC), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
       if (j == 0 && a.bctc_ymin != 0) {
         if (a.bctc_ymin == 1)
-          FLt = ddivc(kL * 2.0 * (TC - a.bctc_ymin_value), a.dy, a.inv_dy, a.dy_pow2);
+          FLt = ddivc(kL * 2.0 * (TC - a.bctc_ymin_value), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
         else
           FLt = kL * a.bctc_ymin_value;
       }
       if (j == a.Ny - 1 && a.bctc_ymax != 0) {
         if (a.bctc_ymax == 1)
-          FRt = ddivc(kR * 2.0 * (a.bctc_ymax_value - TC), a.dy, a.inv_dy, a.dy_pow2);
+          FRt = ddivc(kR * 2.0 * (a.bctc_ymax_value - TC), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
         else
           FRt = kR * a.bctc_ymax_value;
       }
@@ -506,8 +507,8 @@ __global__ void __launch_bounds__(NT, 3)
       cnt_nan += (unsigned)fv_isnan(q.r) + (unsigned)fv_isnan(q.u) + (unsigned)fv_isnan(q.v) + (unsigned)fv_isnan(q.p);
       // inverse hyperbolic dt of the new state (ComputeDt.h:406-409)
       const double cs = sound_speed(q, gas);
-      const double ih = ddivc(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2) +
-                        ddivc(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2);
+      const double ih = ddivc(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx) +
+                        ddivc(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
       lmax = fv_fmax(lmax, ih);
     }
     Qd[g] = q.r;
