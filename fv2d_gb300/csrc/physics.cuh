@@ -114,13 +114,27 @@ __host__ __device__ __forceinline__ bool fv_isnan(float x) { return isnan(x); }
 
 // Products moved from the binary64 pipe to the integer pipes (softfp::mul_rn),
 // by group: the step is bound by the binary64 pipe, and moving every product
-// would make the integer pipes the bound instead.
+// would make the integer pipes the bound instead.  FV2D_SOFT_MUL is a mask
+// (bit GROUP - 1 set: that group on the integer pipes); the groups are
+//   1  HLLC: energies, p gamma, u* numerator, mass and momentum fluxes
+//   2  HLLC: rho/2 (u^2 + v^2)
+//   3  the update's dt (F_L - F_R) products
+//   4  consToPrim: kinetic energy and (E - Ek)(gamma - 1)
+//   5  HLLC: rho (u - S)
+//   6  HLLC: p* numerator
+//   7  HLLC: star state
+//   8  HLLC: energy flux
+//   9  HLL: products of each side's state (kinetic energy, fluxes, momenta)
+//  10  HLL: the HLL average's products by the wave speeds
+//  11  viscous face terms
+//  12  conduction fluxes and the conduction / viscosity update products
+// The default set measured fastest on the Sedov step.
 #ifndef FV2D_SOFT_MUL
-#define FV2D_SOFT_MUL 1
+#define FV2D_SOFT_MUL 269
 #endif
 template <int GROUP, class R>
 __host__ __device__ __forceinline__ R mulx(R a, R b) {
-  if constexpr (FV2D_SOFT_MUL >= GROUP) return fv_mul(a, b);
+  if constexpr ((FV2D_SOFT_MUL >> (GROUP - 1)) & 1) return fv_mul(a, b);
   else return a * b;
 }
 
@@ -164,8 +178,8 @@ __host__ __device__ __forceinline__ S4<R> cons_to_prim(const S4<R> &u, const Gas
   S4<R> q;
   q.r = u.r;
   fv_div2(u.u, u.v, u.r, q.u, q.v);
-  R Ek = mulx<3>(fv_half(q.r), mulx<3>(q.u, q.u) + mulx<3>(q.v, q.v));
-  q.p = mulx<3>(u.p - Ek, g.gm1);
+  R Ek = mulx<4>(fv_half(q.r), mulx<4>(q.u, q.u) + mulx<4>(q.v, q.v));
+  q.p = mulx<4>(u.p - Ek, g.gm1);
   return q;
 }
 
@@ -215,25 +229,25 @@ __device__ __forceinline__ void riemann_hll(const S4<R> &qL, const S4<R> &qR, S4
   // term of primToCons below: the same division, evaluated once.
   const R peL = fv_div_by(qL.p, g.gm1, g.rgm1);
   const R peR = fv_div_by(qR.p, g.gm1, g.rgm1);
-  const R EkL = fv_half(qL.r) * (qL.u * qL.u + qL.v * qL.v);
-  const R EkR = fv_half(qR.r) * (qR.u * qR.u + qR.v * qR.v);
+  const R EkL = mulx<9>(fv_half(qL.r), mulx<9>(qL.u, qL.u) + mulx<9>(qL.v, qL.v));
+  const R EkR = mulx<9>(fv_half(qR.r), mulx<9>(qR.u, qR.u) + mulx<9>(qR.v, qR.v));
   const R EL = (peL + EkL);
   const R ER = (peR + EkR);
-  const R ruL = qL.r * qL.u, ruR = qR.r * qR.u;
-  S4<R> FL{ruL, ruL * qL.u + qL.p, ruL * qL.v, (qL.p + EL) * qL.u};
-  S4<R> FR{ruR, ruR * qR.u + qR.p, ruR * qR.v, (qR.p + ER) * qR.u};
+  const R ruL = mulx<9>(qL.r, qL.u), ruR = mulx<9>(qR.r, qR.u);
+  S4<R> FL{ruL, mulx<9>(ruL, qL.u) + qL.p, mulx<9>(ruL, qL.v), mulx<9>(qL.p + EL, qL.u)};
+  S4<R> FR{ruR, mulx<9>(ruR, qR.u) + qR.p, mulx<9>(ruR, qR.v), mulx<9>(qR.p + ER, qR.u)};
   // primToCons (States.h:19-30) of both states
-  const R mvL = qL.r * qL.v, mvR = qR.r * qR.v;
-  const R uEL = (fv_div_by(fv_half(ruL * ruL + mvL * mvL), qL.r, rL) + peL);
-  const R uER = (fv_div_by(fv_half(ruR * ruR + mvR * mvR), qR.r, rR) + peR);
-  const R SLSR = SL * SR;
+  const R mvL = mulx<9>(qL.r, qL.v), mvR = mulx<9>(qR.r, qR.v);
+  const R uEL = (fv_div_by(fv_half(mulx<9>(ruL, ruL) + mulx<9>(mvL, mvL)), qL.r, rL) + peL);
+  const R uER = (fv_div_by(fv_half(mulx<9>(ruR, ruR) + mulx<9>(mvR, mvR)), qR.r, rR) + peR);
+  const R SLSR = mulx<10>(SL, SR);
   const R den = SR - SL;
   const uint64_t rden = fv_recip(den);
   S4<R> FM;
-  FM.r = fv_div_by(SR * FL.r - SL * FR.r + SLSR * (qR.r - qL.r), den, rden);
-  FM.u = fv_div_by(SR * FL.u - SL * FR.u + SLSR * (ruR - ruL), den, rden);
-  FM.v = fv_div_by(SR * FL.v - SL * FR.v + SLSR * (mvR - mvL), den, rden);
-  FM.p = fv_div_by(SR * FL.p - SL * FR.p + SLSR * (uER - uEL), den, rden);
+  FM.r = fv_div_by(mulx<10>(SR, FL.r) - mulx<10>(SL, FR.r) + mulx<10>(SLSR, qR.r - qL.r), den, rden);
+  FM.u = fv_div_by(mulx<10>(SR, FL.u) - mulx<10>(SL, FR.u) + mulx<10>(SLSR, ruR - ruL), den, rden);
+  FM.v = fv_div_by(mulx<10>(SR, FL.v) - mulx<10>(SL, FR.v) + mulx<10>(SLSR, mvR - mvL), den, rden);
+  FM.p = fv_div_by(mulx<10>(SR, FL.p) - mulx<10>(SL, FR.p) + mulx<10>(SLSR, uER - uEL), den, rden);
   const R pM = fv_half(qL.p + qR.p);
   const bool left = fv_ge0(SL);
   const bool right = !left && fv_le0(SR);
@@ -260,11 +274,11 @@ __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S
   const R cmax = fv_fmax(cL, cR);
   const R SL = fv_fmin(uL, uR) - cmax;
   const R SR = fv_fmax(uL, uR) + cmax;
-  const R rcL = mulx<2>(rL, uL - SL);
-  const R rcR = mulx<2>(rR, SR - uR);
+  const R rcL = mulx<5>(rL, uL - SL);
+  const R rcR = mulx<5>(rR, SR - uR);
   R uS, pS;
   fv_div2(mulx<1>(rcR, uR) + mulx<1>(rcL, uL) + (pL - pR),
-          mulx<2>(rcR, pL) + mulx<2>(rcL, pR) + mulx<2>(mulx<2>(rcL, rcR), uL - uR), rcR + rcL, uS, pS);
+          mulx<6>(rcR, pL) + mulx<6>(rcL, pR) + mulx<6>(mulx<6>(rcL, rcR), uL - uR), rcR + rcL, uS, pS);
   const bool sideL = fv_gt0(uS);
   const R rK = sideL ? rL : rR;
   const R uK = sideL ? uL : uR;
@@ -272,7 +286,7 @@ __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S
   const R EK = sideL ? EL : ER;
   const R SK = sideL ? SL : SR;
   R rS, ES;
-  fv_div2(mulx<2>(rK, SK - uK), mulx<2>(SK - uK, EK) - mulx<2>(pK, uK) + mulx<2>(pS, uS), SK - uS, rS, ES);
+  fv_div2(mulx<7>(rK, SK - uK), mulx<7>(SK - uK, EK) - mulx<7>(pK, uK) + mulx<7>(pS, uS), SK - uS, rS, ES);
   // branch order of RiemannSolvers.h:89-112
   const bool bL = fv_gt0(SL);
   const bool bStar = !bL && (sideL || fv_gt0(SR));
@@ -288,7 +302,7 @@ __device__ __forceinline__ void riemann_hllc(const S4<R> &qL, const S4<R> &qR, S
   f.r = mulx<1>(sr, su);
   f.u = mulx<1>(mulx<1>(sr, su), su) + sp;
   f.v = mulx<1>(f.r, sv);
-  f.p = mulx<2>(E + sp, su);
+  f.p = mulx<8>(E + sp, su);
 }
 
 // RiemannSolvers.h:130-171 (Kokkos::max / min as (a<b)?b:a and (b<a)?b:a).

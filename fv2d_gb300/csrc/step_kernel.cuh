@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(NT, 3)
     constexpr double two_thirds = 2.0 / 3.0;
     const double mu = a.mu;
     const double odx = a.one_over_dx, ody = a.one_over_dy;
+    const double q_odx = 0.25 * odx, q_ody = 0.25 * ody;  // (0.25 * ody) * (...) as the reference groups it
     constexpr int NVX = TY * (TX + 1), NVY = (TY + 1) * TX;
     for (int f = tid; f < NVX + NVY; f += NT) {
       if (f < NVX) {  // between columns c+1 (s-1) and c+2 (s) of row r+2
@@ -345,15 +346,15 @@ __global__ void __launch_bounds__(NT, 3)
         auto V_ = [&](int dj, int x) { return sQ(2, ly + dj, x); };
         const double qiu = fv_half(U_(0, xs) + U_(0, xm));
         const double qiv = fv_half(V_(0, xs) + V_(0, xm));
-        const double dudx = odx * (U_(0, xs) - U_(0, xm));
-        const double dvdx = odx * (V_(0, xs) - V_(0, xm));
-        const double dudy = 0.25 * ody * (U_(1, xs) - U_(-1, xs) + U_(1, xm) - U_(-1, xm));
-        const double dvdy = 0.25 * ody * (V_(1, xs) - V_(-1, xs) + V_(1, xm) - V_(-1, xm));
-        const double tau_xx = four_thirds * dudx - two_thirds * dvdy;
+        const double dudx = mulx<11>(odx, U_(0, xs) - U_(0, xm));
+        const double dvdx = mulx<11>(odx, V_(0, xs) - V_(0, xm));
+        const double dudy = mulx<11>(q_ody, U_(1, xs) - U_(-1, xs) + U_(1, xm) - U_(-1, xm));
+        const double dvdy = mulx<11>(q_ody, V_(1, xs) - V_(-1, xs) + V_(1, xm) - V_(-1, xm));
+        const double tau_xx = mulx<11>(four_thirds, dudx) - mulx<11>(two_thirds, dvdy);
         const double tau_xy = dvdx + dudy;
-        SMI(L::VX + f) = mu * tau_xx;
-        SMI(L::VX + f + NVX) = mu * tau_xy;
-        SMI(L::VX + f + 2 * NVX) = mu * (tau_xx * qiu + tau_xy * qiv);
+        SMI(L::VX + f) = mulx<11>(mu, tau_xx);
+        SMI(L::VX + f + NVX) = mulx<11>(mu, tau_xy);
+        SMI(L::VX + f + 2 * NVX) = mulx<11>(mu, mulx<11>(tau_xx, qiu) + mulx<11>(tau_xy, qiv));
       } else {  // between rows r+1 (s-1) and r+2 (s) of column c+2
         const int g = f - NVX;
         const int r = g / TX, c = g % TX;
@@ -362,15 +363,15 @@ __global__ void __launch_bounds__(NT, 3)
         auto V_ = [&](int y, int di) { return sQ(2, y, lx + di); };
         const double qiu = fv_half(U_(ys, 0) + U_(ym, 0));
         const double qiv = fv_half(V_(ys, 0) + V_(ym, 0));
-        const double dudy = ody * (U_(ys, 0) - U_(ym, 0));
-        const double dvdy = ody * (V_(ys, 0) - V_(ym, 0));
-        const double dudx = 0.25 * odx * (U_(ys, 1) - U_(ys, -1) + U_(ym, 1) - U_(ym, -1));
-        const double dvdx = 0.25 * odx * (V_(ys, 1) - V_(ys, -1) + V_(ym, 1) - V_(ym, -1));
-        const double tau_yy = four_thirds * dvdy - two_thirds * dudx;
+        const double dudy = mulx<11>(ody, U_(ys, 0) - U_(ym, 0));
+        const double dvdy = mulx<11>(ody, V_(ys, 0) - V_(ym, 0));
+        const double dudx = mulx<11>(q_odx, U_(ys, 1) - U_(ys, -1) + U_(ym, 1) - U_(ym, -1));
+        const double dvdx = mulx<11>(q_odx, V_(ys, 1) - V_(ys, -1) + V_(ym, 1) - V_(ym, -1));
+        const double tau_yy = mulx<11>(four_thirds, dvdy) - mulx<11>(two_thirds, dudx);
         const double tau_xy = dvdx + dudy;
-        SMI(L::VY + g) = mu * tau_xy;
-        SMI(L::VY + g + NVY) = mu * tau_yy;
-        SMI(L::VY + g + 2 * NVY) = mu * (tau_xy * qiu + tau_yy * qiv);
+        SMI(L::VY + g) = mulx<11>(mu, tau_xy);
+        SMI(L::VY + g + NVY) = mulx<11>(mu, tau_yy);
+        SMI(L::VY + g + 2 * NVY) = mulx<11>(mu, mulx<11>(tau_xy, qiu) + mulx<11>(tau_yy, qiv));
       }
     }
   }
@@ -449,10 +450,10 @@ __global__ void __launch_bounds__(NT, 3)
       const double TU = sR1(L::T, 0, ly - 1, lx), TD = sR1(L::T, 0, ly + 1, lx);
       const double kL = a.kap_row[4 * j + 0], kR = a.kap_row[4 * j + 1];
       const double kU = a.kap_row[4 * j + 2], kD = a.kap_row[4 * j + 3];
-      double FLt = ddivc(kL * (TC - TL), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx);
-      double FRt = ddivc(kR * (TR - TC), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx);
-      const double FUt = ddivc(kU * (TC - TU), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
-      const double FDt = ddivc(kD * (TD - TC), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
+      double FLt = ddivc(mulx<12>(kL, TC - TL), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx);
+      double FRt = ddivc(mulx<12>(kR, TR - TC), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx);
+      const double FUt = ddivc(mulx<12>(kU, TC - TU), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
+      const double FDt = ddivc(mulx<12>(kD, TD - TC), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
       if (j == 0 && a.bctc_ymin != 0) {
         if (a.bctc_ymin == 1)
           FLt = ddivc(kL * 2.0 * (TC - a.bctc_ymin_value), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);
@@ -465,7 +466,7 @@ __global__ void __launch_bounds__(NT, 3)
         else
           FRt = kR * a.bctc_ymax_value;
       }
-      un[3] += s_tc[0] * (FRt - FLt) + s_tc[1] * (FDt - FUt);
+      un[3] += mulx<12>(s_tc[0], FRt - FLt) + mulx<12>(s_tc[1], FDt - FUt);
     }
     // viscosity (Viscosity.h:148-228): the face terms of the face pass, the
     // -side face negated, accumulated in the reference's order
@@ -487,9 +488,9 @@ __global__ void __launch_bounds__(NT, 3)
       fy2 += SMI(Vn + NVY + TX);
       fy3 += SMI(Vn + 2 * NVY + TX);
       un[0] += (0.0 + 0.0) * dt;
-      un[1] += (fx1 + fy1) * dt;
-      un[2] += (fx2 + fy2) * dt;
-      un[3] += (fx3 + fy3) * dt;
+      un[1] += mulx<12>(fx1 + fy1, dt);
+      un[2] += mulx<12>(fx2 + fy2, dt);
+      un[3] += mulx<12>(fx3 + fy3, dt);
     }
     // RK2 corrector: 0.5 * (U0 + Unew) (Update.h:214-220)
     if (a.stage == STAGE_RK2_CORRECT) {
