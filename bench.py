@@ -248,6 +248,85 @@ def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, de
     }
 
 
+def binary32_rounded_state(q, gamma):
+    """Primitive state whose conservative form is q's rounded to binary32:
+    the rounding the service applies when it admits a request
+    (States.h:20-30 forward, States.h:33-43 back, both in binary64)."""
+    r, u, v, p = (q[..., k] for k in range(4))
+    U = np.stack([r, r * u, r * v, p / (gamma - 1.0) + 0.5 * r * (u * u + v * v)], axis=-1)
+    U = U.astype(np.float32).astype(np.float64)
+    r2 = U[..., 0]
+    out = np.empty_like(q)
+    out[..., 0] = r2
+    out[..., 1] = U[..., 1] / r2
+    out[..., 2] = U[..., 2] / r2
+    out[..., 3] = (U[..., 3] - 0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2) / r2) * (gamma - 1.0)
+    return out
+
+
+def served_accuracy(fv, sample_every=16, device=0):
+    """Accuracy of the batched FP32 service on the stream sample (every 16th
+    request), request by request, against the plain FP64 path (bit-identical
+    to the reference) run from the same initial condition, beside two
+    sensitivity floors of each problem measured with the FP64 path alone:
+    the initial density perturbed by one binary64 ulp, and the initial
+    state rounded to binary32 as the service stores it.  L1 errors are
+    sum |a - b| / sum |b| over the interior."""
+    from fv2d_gb300.serve import Server, stream_requests
+    reqs = stream_requests()
+    sub = list(range(0, len(reqs), sample_every))
+    with Server(budget_bytes=60e9, device=device, autotune=False) as srv:
+        ids = {srv.submit(reqs[i]["problem"], reqs[i]["params"], reqs[i]["steps"], lowmach=reqs[i]["lowmach"]): i
+               for i in sub}
+        if srv.drain(900) != 0:
+            raise RuntimeError("the service did not finish the sample")
+        res = {ids[x.id]: x for x in srv.poll()}
+        q32 = {i: srv.get_prim(x.id) for i, x in res.items()}
+
+    def l1(a, b, k):
+        return float(np.sum(np.abs(a[..., k] - b[..., k])) / np.sum(np.abs(b[..., k])))
+
+    rows = []
+    for i in sub:
+        r = reqs[i]
+        p = r["params"]
+
+        def run(q0=None):
+            sim = fv.Simulation(p, device=device)
+            sim.init_problem(r["problem"])
+            if q0 is not None:
+                sim.set_prim(q0)
+            sim.advance(r["steps"], 1e30)
+            q = sim.get_prim()
+            sim.close()
+            return q
+
+        s0 = fv.Simulation(p, device=device)
+        s0.init_problem(r["problem"])
+        q_ic = s0.get_prim()
+        s0.close()
+        q64 = run()
+        q_ulp = q_ic.copy()
+        q_ulp[..., 0] = np.nextafter(q_ulp[..., 0], np.inf)
+        q_ulp = run(q_ulp)
+        q_f32ic = run(binary32_rounded_state(q_ic, p.gamma0))
+        x = res[i]
+        row = {"kind": r["kind"], "N": r["N"], "steps": r["steps"], "status": x.status,
+               "l1_rho": l1(q32[i], q64, 0), "l1_p": l1(q32[i], q64, 3),
+               "fp64_1ulp_l1_rho": l1(q_ulp, q64, 0), "fp64_f32_ic_l1_rho": l1(q_f32ic, q64, 0),
+               "fp64_f32_ic_l1_p": l1(q_f32ic, q64, 3)}
+        if r["kind"] != "sod":  # closed domains: binary64 sums of the binary32 state
+            row["mass_drift"] = abs(x.cons1[0] - x.cons0[0]) / abs(x.cons0[0])
+        rows.append(row)
+    med = {k: float(np.median([w[k] for w in rows]))
+           for k in ("l1_rho", "l1_p", "fp64_1ulp_l1_rho", "fp64_f32_ic_l1_rho")}
+    summary = {"served_accuracy": True, "sample": len(rows), "median": med,
+               "l1_rho_le_1e-5": sum(w["l1_rho"] <= 1e-5 for w in rows),
+               "l1_rho_within_10x_f32_ic_floor": sum(w["l1_rho"] <= 10 * w["fp64_f32_ic_l1_rho"] for w in rows),
+               "mass_drift_max": max(w.get("mass_drift", 0.0) for w in rows)}
+    return rows, summary
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -297,6 +376,8 @@ def main():
                     help="fixed batch for kernel profiling: 12 Sedov 768^2 requests x 60 steps")
     ap.add_argument("--served-saturated", action="store_true",
                     help="service rate without arrival gaps: the request stream submitted at once")
+    ap.add_argument("--served-accuracy", action="store_true",
+                    help="per-request accuracy of the service on the stream sample against the FP64 path")
     ap.add_argument("--served-tile", default=None,
                     help="kernel configuration for every bucket of the profiling batch (e.g. 28x64/128/march)")
     args = ap.parse_args()
@@ -334,6 +415,12 @@ def main():
                               "p50_s": float(np.median(lat)), "p99_s": float(np.percentile(lat, 99)),
                               "tile_configs_per_bucket": [config_name(st.bucket_cfg[b]) for b in range(4)]}),
                   flush=True)
+        return
+    if args.served_accuracy:
+        rows, summary = served_accuracy(fv, device=local)
+        for w in rows:
+            print(json.dumps(w), flush=True)
+        print(json.dumps(summary), flush=True)
         return
     if args.served_profile:
         from fv2d_gb300.serve import Server
