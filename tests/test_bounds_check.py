@@ -1,7 +1,7 @@
 """The bounds-check build (-DFV2D_BOUNDS_CHECK; compute-sanitizer is not used
 here): every shared-memory index and global plane index of the FP64 step is
 checked on the device, a bad one recorded in the context's error bits and
-skipped.  On odd grid sizes that cut tiles and on every kind of step
+skipped.  On odd grid sizes that cut tiles (down to two cells along an axis) and on every kind of step
 (PCM / PLM / MUSCL-Hancock, HLL / HLLC / FSLP, Euler / RK2, gravity,
 conduction, viscosity, the well-balanced boundary flux, every boundary type)
 it must report nothing and produce the same bits as the normal build."""
@@ -18,7 +18,7 @@ from fv2d_testlib import bits_equal, random_prim, reference_params
 pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SHAPES = [(5, 3), (17, 33), (40, 65)]
+SHAPES = [(5, 3), (17, 33), (40, 65), (2, 2), (2, 9), (9, 2)]
 
 
 def cases():

@@ -82,7 +82,7 @@ def test_sod_granular_calls_match_device_loop(gpu_lib):
     assert bits_equal(a.get_cons(), b.get_cons())
 
 
-@pytest.mark.parametrize("shape", [(17, 33), (40, 65), (37, 100), (5, 3)])
+@pytest.mark.parametrize("shape", [(17, 33), (40, 65), (37, 100), (5, 3), (2, 2), (2, 9), (9, 2)])
 def test_odd_sizes_match_oracle(gpu_lib, shape):
     ny, nx = shape
     q0 = random_prim(ny, nx, 11 + nx)

@@ -92,6 +92,28 @@ def test_against_reference_headers(seed):
 
 
 @pytest.mark.skipif(not ref_available(), reason="reference cross-check build (oracle/_ref) not present")
+@pytest.mark.parametrize("shape", [(2, 2), (2, 9), (9, 2)])
+def test_smallest_grids_against_reference_headers(shape):
+    """Grids of two cells along an axis: every ghost copies an interior cell
+    (BoundaryConditions.h:22-71 with Nghosts = 2), every combination."""
+    ny, nx = shape
+    q0 = random_prim(ny, nx, 13)
+    for c in G.combo_list()[::3]:
+        p = reference_params(Nx=nx, Ny=ny, gamma0=1.4, CFL=0.6, **c)
+        o, r = Oracle(p), RefSim(p)
+        o.set_prim(q0)
+        r.set_prim(q0)
+        for _ in range(3):
+            d = o.compute_dt()
+            dr = r.compute_dt()
+            assert bits_equal(d[0], dr), c
+            o.update(d[0])
+            r.update(dr)
+        assert bits_equal(o.get_prim(), r.get_prim()), c
+        assert bits_equal(o.get_cons(), r.get_cons()), c
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference cross-check build (oracle/_ref) not present")
 def test_reference_reads_floats():
     """The reference's ini reader returns float-rounded reals (GetFloat)."""
     p = reference_params(Nx=8, Ny=8, gamma0=1.4, CFL=0.8)
