@@ -34,6 +34,9 @@ static const BatchCfg kCfgs[] = {
     FV2D_MARCH(64, 128, 4, "28x64/128/march"),
     FV2D_MARCH(32, 128, 5, "28x32/128x5/march"),
     FV2D_MARCH(64, 128, 5, "28x64/128x5/march"),
+    FV2D_MARCH(32, 64, 8, "28x32/64/march"),
+    FV2D_MARCH(64, 64, 8, "28x64/64/march"),
+    FV2D_MARCH(64, 96, 5, "28x64/96/march"),
 };
 
 int batch_num_cfgs() { return (int)(sizeof(kCfgs) / sizeof(kCfgs[0])); }

@@ -39,7 +39,7 @@ def mixed_requests():
 
 
 # the default tile kernel and the register-resident column-marching kernel
-TILES = [None, "28x64/128/march"]
+TILES = [None, "28x64/128/march", "28x32/64/march"]
 
 
 @pytest.mark.parametrize("tile", TILES)
