@@ -166,7 +166,7 @@ def cpu_oracle_rate(n, steps_cap=20, budget_s=15.0):
                       f"reference pass structure, -O3 -ffp-contract=off)", "seconds": el}
 
 
-def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, device=0):
+def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, device=0, active_cells=8e6):
     """The batched FP32 service on the seeded request stream: requests are
     submitted at their Poisson arrival times; every 16th request is also run
     alone through the plain FP64 path (bit-identical to the reference) for
@@ -174,7 +174,7 @@ def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, de
     from fv2d_gb300.serve import Server, stream_requests, config_name
     reqs = stream_requests(n=n_requests, rate=rate)
     sample = set(range(0, len(reqs), sample_every))
-    srv = Server(budget_bytes=budget, device=device, autotune=True)
+    srv = Server(budget_bytes=budget, device=device, autotune=True, active_cells=active_cells)
     st0 = srv.stats()
     results, ids, keep = {}, {}, {}
     t_start = time.perf_counter()
@@ -237,6 +237,8 @@ def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, de
         "f64 clock/dt/conservation sums/low-Mach energy recovery", "wall_s": wall, "cell_updates": work,
         "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
         "tile_configs_per_bucket": cfgs, "replays": st.replays, "arena_reserved_gb": st.bytes_reserved / 1e9,
+        "scheduling": ("shortest remaining work first, about %.3g cells per step" % active_cells) if active_cells > 0
+        else "every admitted request at every step",
         "plain_fp64_one_at_a_time": {"sample": len(sub), "aggregate": plain_rate, "unit": METRIC,
                                      "p50_s": float(np.percentile(tts64, 50)),
                                      "p99_s": float(np.percentile(tts64, 99)),
@@ -386,6 +388,9 @@ def main():
                     help="service rate without arrival gaps: the request stream submitted at once")
     ap.add_argument("--served-accuracy", action="store_true",
                     help="per-request accuracy of the service on the stream sample against the FP64 path")
+    ap.add_argument("--served-active-cells", type=float, default=8e6,
+                    help="service scheduling: shortest remaining work first with about this many cells per step "
+                         "(0: every admitted request advances at every step)")
     ap.add_argument("--served-tile", default=None,
                     help="kernel configuration for every bucket of the profiling batch (e.g. 28x64/128/march)")
     args = ap.parse_args()
@@ -405,7 +410,7 @@ def main():
         from fv2d_gb300.serve import Server, stream_requests, config_name
         reqs = stream_requests(n=args.served_requests)
         with Server(budget_bytes=150e9, device=local, autotune=args.served_tile is None,
-                    tile_config=args.served_tile) as srv:
+                    tile_config=args.served_tile, active_cells=args.served_active_cells) as srv:
             t0 = time.perf_counter()
             for r in reqs:
                 srv.submit(r["problem"], r["params"], r["steps"], lowmach=r["lowmach"])
@@ -421,6 +426,7 @@ def main():
             print(json.dumps({"served_saturated": True, "requests": len(reqs), "cell_updates": work,
                               "wall_s": wall, "rate": work / wall, "unit": METRIC,
                               "p50_s": float(np.median(lat)), "p99_s": float(np.percentile(lat, 99)),
+                              "active_cells": args.served_active_cells,
                               "tile_configs_per_bucket": [config_name(st.bucket_cfg[b]) for b in range(4)]}),
                   flush=True)
         return
@@ -443,7 +449,8 @@ def main():
         return
     if args.served_only:
         t0 = time.perf_counter()
-        served = run_served(fv, n_requests=args.served_requests, device=local)
+        served = run_served(fv, n_requests=args.served_requests, device=local,
+                            active_cells=args.served_active_cells)
         print(json.dumps({"metric": METRIC, "served": served, "wall_s": time.perf_counter() - t0}), flush=True)
         return
     torch.cuda.set_device(local)
@@ -590,7 +597,8 @@ def main():
     served = None
     if world == 1 and not args.no_served:
         import numpy  # noqa: F401
-        served = run_served(fv, n_requests=args.served_requests, device=local)
+        served = run_served(fv, n_requests=args.served_requests, device=local,
+                            active_cells=args.served_active_cells)
 
     if rank != 0:
         return

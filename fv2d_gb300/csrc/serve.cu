@@ -286,6 +286,10 @@ struct fv2d_server {
   int replays = 0;
   double rate_est = 2e10;  // cell-updates/s, refined by measurement
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the buckets' step chains run as parallel branches of a replay graph
+  cudaStream_t bstream[kBuckets] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kBuckets] = {};
+  double sched_cells = 0;  // cells advanced per step by the current work lists
   std::string err;
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
@@ -461,13 +465,47 @@ void read_initial_cons(fv2d_server *s, const std::vector<int> &fresh) {
   }
 }
 
+// Remaining cell-updates of a resident request: its remaining steps (the
+// step limit, or the time limit at the last dt when that comes first) times
+// its cells.
+double remaining_work(const fv2d_server *s, int slot) {
+  const Slot &sl = s->slots[slot];
+  const double cells = (double)sl.req.params.Nx * sl.req.params.Ny;
+  double steps = (double)sl.req.max_steps - sl.steps_seen;
+  if (sl.steps_seen > 0 && sl.req.tend > 0) {
+    const SimDev &d = s->h_down[slot];
+    if (d.dt > 0) steps = std::min(steps, std::ceil((sl.req.tend - d.t) / d.dt));
+  }
+  return std::max(steps, 1.0) * cells;
+}
+
 void rebuild_lists(fv2d_server *s) {
   std::vector<WorkItem> lists[kBuckets];
+  std::vector<int> run;
+  for (int k = 0; k < s->max_sims; ++k)
+    if (s->slots[k].used) run.push_back(k);
+  if (s->cfg.active_cells > 0) {
+    // shortest remaining work first, up to about active_cells cells per step
+    std::vector<std::pair<double, int>> order;
+    for (int k : run) order.emplace_back(remaining_work(s, k), k);
+    std::sort(order.begin(), order.end());
+    run.clear();
+    double cells = 0;
+    for (const auto &o : order) {
+      if (!run.empty() && cells >= s->cfg.active_cells) break;
+      run.push_back(o.second);
+      cells += (double)s->slots[o.second].req.params.Nx * s->slots[o.second].req.params.Ny;
+    }
+    std::sort(run.begin(), run.end());
+  }
   // interleave tiles of the simulations of a bucket so that a CTA's
   // consecutive items belong to different simulations
   std::vector<int> per_bucket[kBuckets];
-  for (int k = 0; k < s->max_sims; ++k)
-    if (s->slots[k].used) per_bucket[s->slots[k].bucket].push_back(k);
+  s->sched_cells = 0;
+  for (int k : run) {
+    per_bucket[s->slots[k].bucket].push_back(k);
+    s->sched_cells += (double)s->slots[k].req.params.Nx * s->slots[k].req.params.Ny;
+  }
   s->mask = 0;
   for (int b = 0; b < kBuckets; ++b) {
     for (int slot : per_bucket[b]) {
@@ -516,7 +554,19 @@ cudaGraphExec_t get_graph(fv2d_server *s, int K, int mask) {
   if (it != s->graphs.end()) return it->second;
   cudaGraph_t g;
   if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
-  for (int k = 0; k < K; ++k) launch_step(s, mask);
+  // one branch per bucket: a request's steps depend only on its own previous
+  // step, so the buckets' chains are independent and a small bucket's
+  // kernels can fill the SMs that a large one's leave idle
+  cudaEventRecord(s->ev_fork, s->stream);
+  for (int b = 0; b < kBuckets; ++b) {
+    if (!(mask & (1 << b))) continue;
+    cudaStreamWaitEvent(s->bstream[b], s->ev_fork, 0);
+    BatchArgs a{s->d_sims, s->d_work[b], s->d_nwork + b, s->d_tmaps};
+    const int c = s->bucket_cfg[b];
+    for (int k = 0; k < K; ++k) batch_launch(c, s->cfg_grid[c], s->bstream[b], a);
+    cudaEventRecord(s->ev_join[b], s->bstream[b]);
+    cudaStreamWaitEvent(s->stream, s->ev_join[b], 0);
+  }
   if (cudaStreamEndCapture(s->stream, &g) != cudaSuccess) return nullptr;
   cudaGraphExec_t ex = nullptr;
   if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ex = nullptr;
@@ -609,17 +659,16 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
 bool run_once(fv2d_server *s, int K_fixed) {
   const NvtxRange nvtx_range("fv2d_server replay");
   bool any = false;
-  double active_cells = 0;
   for (int k = 0; k < s->max_sims; ++k)
     if (s->slots[k].used) {
       any = true;
-      active_cells += (double)s->slots[k].req.params.Nx * s->slots[k].req.params.Ny;
+      break;
     }
   if (!any) return false;
   if (s->lists_dirty) rebuild_lists(s);
   int K = K_fixed;
   if (K <= 0) {
-    const double step_s = active_cells / s->rate_est;
+    const double step_s = s->sched_cells / s->rate_est;
     K = 1;
     while (K < 64 && (K * 2) * step_s < 3e-3) K *= 2;
   }
@@ -774,6 +823,7 @@ const char *fv2d_server_config_name(int index) {
 int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   if (!cfg || !out || cfg->struct_size != sizeof(fv2d_server_config)) return FV2D_ERR_INVALID;
   if (cfg->max_sims <= 0 || cfg->max_sims > 16384 || !(cfg->budget_bytes > 0)) return FV2D_ERR_INVALID;
+  if (!(cfg->active_cells >= 0) || std::isinf(cfg->active_cells)) return FV2D_ERR_INVALID;
   *out = nullptr;
   fv2d_server *s = new (std::nothrow) fv2d_server();
   if (!s) return FV2D_ERR_NOMEM;
@@ -797,7 +847,11 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
             cudaMallocHost(&s->h_nwork, sizeof(int) * kBuckets) == cudaSuccess &&
             cudaMalloc(&s->d_cons, sizeof(double) * kConsBlocks * 8 * s->max_sims) == cudaSuccess &&
             cudaMallocHost(&s->h_cons, sizeof(double) * kConsBlocks * 8 * s->max_sims) == cudaSuccess &&
-            cudaEventCreate(&s->ev0) == cudaSuccess && cudaEventCreate(&s->ev1) == cudaSuccess;
+            cudaEventCreate(&s->ev0) == cudaSuccess && cudaEventCreate(&s->ev1) == cudaSuccess &&
+            cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int b = 0; ok && b < kBuckets; ++b)
+    ok = cudaStreamCreateWithFlags(&s->bstream[b], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&s->ev_join[b], cudaEventDisableTiming) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     fv2d_server_destroy(s);
@@ -847,6 +901,11 @@ int fv2d_server_destroy(fv2d_server *s) {
   if (s->h_stage) cudaFreeHost(s->h_stage);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  for (int b = 0; b < kBuckets; ++b) {
+    if (s->ev_join[b]) cudaEventDestroy(s->ev_join[b]);
+    if (s->bstream[b]) cudaStreamDestroy(s->bstream[b]);
+  }
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return FV2D_OK;

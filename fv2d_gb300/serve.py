@@ -12,7 +12,7 @@ from ._abi import Params, PROBLEMS, as_float32
 class ServerConfig(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("device", C.c_int32), ("budget_bytes", C.c_double),
                 ("max_sims", C.c_int32), ("autotune", C.c_int32), ("steps_per_replay", C.c_int32),
-                ("tile_config", C.c_int32)]
+                ("tile_config", C.c_int32), ("active_cells", C.c_double)]
 
 
 class Request(C.Structure):
@@ -78,9 +78,12 @@ class Server:
     """A running batched service on one GPU."""
 
     def __init__(self, budget_bytes=150e9, device=0, max_sims=4096, autotune=True, steps_per_replay=0,
-                 tile_config=None):
+                 tile_config=None, active_cells=0.0):
         """tile_config: name of a kernel configuration (config_name) to use for
-        every grid-size bucket instead of the defaults or the autotuner."""
+        every grid-size bucket instead of the defaults or the autotuner.
+        active_cells: 0 advances every admitted request at every step; a
+        positive value schedules shortest remaining work first, about that
+        many cells per step."""
         self.L = _bind(_lib_loader())
         forced = 0
         if tile_config is not None:
@@ -89,7 +92,7 @@ class Server:
                 raise ValueError(f"unknown tile configuration {tile_config!r}; known: {names}")
             forced = names.index(tile_config) + 1
         cfg = ServerConfig(C.sizeof(ServerConfig), device, float(budget_bytes), max_sims, 1 if autotune else 0,
-                           steps_per_replay, forced)
+                           steps_per_replay, forced, float(active_cells))
         self.h = C.c_void_p()
         rc = self.L.fv2d_server_create(C.byref(cfg), C.byref(self.h))
         if rc != 0:

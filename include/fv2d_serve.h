@@ -42,6 +42,10 @@ typedef struct fv2d_server_config {
   int32_t autotune;         /* 1: time the tile configurations per bucket at start-up */
   int32_t steps_per_replay; /* 0: adaptive (about 3 ms of work per graph replay) */
   int32_t tile_config;      /* 0: defaults or autotuned; k > 0: configuration k - 1 for every bucket */
+  double active_cells;      /* 0: every admitted request advances at every step.  > 0: shortest remaining
+                               work first -- the requests with the fewest remaining cell-updates advance,
+                               about this many cells per step (at least one request); the others stay
+                               resident in HBM until they rank among them */
 } fv2d_server_config;
 
 typedef struct fv2d_request {

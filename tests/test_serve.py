@@ -42,8 +42,11 @@ def mixed_requests():
 TILES = [None, "28x64/128/march", "28x32/64/march"]
 
 
+@pytest.mark.parametrize("active", [0.0, 3e5])
 @pytest.mark.parametrize("tile", TILES)
-def test_same_result_alone_and_in_the_mix(gpu_lib, tile):
+def test_same_result_alone_and_in_the_mix(gpu_lib, tile, active):
+    """active > 0: shortest remaining work first with a cap small enough that
+    requests wait resident while others advance, and resume later."""
     from fv2d_gb300.serve import Server
     reqs = mixed_requests()
     alone = []
@@ -54,7 +57,7 @@ def test_same_result_alone_and_in_the_mix(gpu_lib, tile):
             res = {r.id: r for r in s.poll()}
             assert res[rid].status == 0 and res[rid].steps == n
             alone.append((s.get_prim(rid), res[rid].t))
-    with Server(budget_bytes=4e9, autotune=False, tile_config=tile) as s:
+    with Server(budget_bytes=4e9, autotune=False, tile_config=tile, active_cells=active) as s:
         fillers = [s.submit("sedov", params(N), 30 + N // 16) for N in (64, 320, 512, 192, 96)]
         ids = [s.submit(pb, p, n, lowmach=lm) for pb, p, n, lm in reqs]
         fillers += [s.submit("kh_step", params(N, boundary_x=2, boundary_y=2), 45) for N in (128, 224)]
