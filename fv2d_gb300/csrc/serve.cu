@@ -263,6 +263,7 @@ struct fv2d_server {
   int *d_nwork = nullptr, *h_nwork = nullptr;
   WorkItem *h_work[kBuckets] = {};
   int work_cap[kBuckets] = {};
+  int items_in[kBuckets] = {};  // work items of the resident requests, per bucket
   int bucket_cfg[kBuckets] = {1, 2, 3, 3};
   int cfg_grid[16] = {};
   bool lists_dirty = true;
@@ -335,8 +336,34 @@ size_t state_bytes(int N, int *pitch, long long *plane) {
   return sizeof(float) * 8 * (size_t)*plane;  // two buffers x four planes
 }
 
+// Grow bucket b's work-list buffers to hold `need` items.  New buffers are
+// allocated before the old ones are released, so a failure leaves the lists
+// as they were.
+bool reserve_work(fv2d_server *s, int b, int need) {
+  if (need <= s->work_cap[b]) return true;
+  int cap = std::max(1024, s->work_cap[b]);
+  while (cap < need) cap *= 2;
+  WorkItem *d = nullptr, *h = nullptr;
+  if (cudaMalloc(&d, sizeof(WorkItem) * cap) != cudaSuccess ||
+      cudaMallocHost(&h, sizeof(WorkItem) * cap) != cudaSuccess) {
+    cudaGetLastError();
+    if (d) cudaFree(d);
+    return false;
+  }
+  cudaStreamSynchronize(s->stream);  // the next rebuild fills the new lists
+  if (s->d_work[b]) cudaFree(s->d_work[b]);
+  if (s->h_work[b]) cudaFreeHost(s->h_work[b]);
+  s->d_work[b] = d;
+  s->h_work[b] = h;
+  s->work_cap[b] = cap;
+  for (auto &g : s->graphs) cudaGraphExecDestroy(g.second);  // kernel arguments changed
+  s->graphs.clear();
+  s->lists_dirty = true;
+  return true;
+}
+
 // Admit one request into a free slot; returns the slot, or -1 when it does
-// not fit.
+// not fit (HBM budget, table or work-list capacity).
 int admit(fv2d_server *s, const Pending &pd) {
   const NvtxRange nvtx_range("fv2d_server admit");
   if (s->free_slots.empty()) return -1;
@@ -346,24 +373,28 @@ int admit(fv2d_server *s, const Pending &pd) {
   int pitch;
   long long plane;
   const size_t bytes = state_bytes(N, &pitch, &plane);
+  const int bucket = bucket_of(N);
+  int tx, ty, nt, staging;
+  batch_cfg_info(s->bucket_cfg[bucket], &tx, &ty, &nt, &staging, nullptr, nullptr);
+  const int items = ((N + tx - 1) / tx) * ((N + ty - 1) / ty);
+  if (!reserve_work(s, bucket, s->items_in[bucket] + items)) return -1;
   void *mem = s->arena.alloc(bytes);
   if (!mem) return -1;
+  s->items_in[bucket] += items;
   const int slot = s->free_slots.back();
   s->free_slots.pop_back();
   Slot &sl = s->slots[slot];
   sl.used = true;
   sl.id = pd.id;
   sl.req = r;
-  sl.bucket = bucket_of(N);
-  sl.cfg = s->bucket_cfg[sl.bucket];
+  sl.bucket = bucket;
+  sl.cfg = s->bucket_cfg[bucket];
   sl.mem = mem;
   sl.bytes = bytes;
   sl.submit_s = pd.submit_s;
   sl.admit_s = s->now();
   sl.cells_done = 0;
   sl.steps_seen = 0;
-  int tx, ty, nt, staging;
-  batch_cfg_info(sl.cfg, &tx, &ty, &nt, &staging, nullptr, nullptr);
 
   SimDev &d = s->h_up[slot];
   std::memset(&d, 0, sizeof(d));
@@ -514,19 +545,8 @@ void rebuild_lists(fv2d_server *s) {
         for (int tx = 0; tx < d.ntx; ++tx) lists[b].push_back(WorkItem{slot, (short)tx, (short)ty});
     }
     if (!lists[b].empty()) s->mask |= 1 << b;
-    const int n = (int)lists[b].size();
-    if (n > s->work_cap[b]) {
-      int cap = std::max(1024, s->work_cap[b]);
-      while (cap < n) cap *= 2;
-      cudaStreamSynchronize(s->stream);
-      if (s->d_work[b]) cudaFree(s->d_work[b]);
-      if (s->h_work[b]) cudaFreeHost(s->h_work[b]);
-      cudaMalloc(&s->d_work[b], sizeof(WorkItem) * cap);
-      cudaMallocHost(&s->h_work[b], sizeof(WorkItem) * cap);
-      s->work_cap[b] = cap;
-      for (auto &g : s->graphs) cudaGraphExecDestroy(g.second);  // kernel arguments changed
-      s->graphs.clear();
-    }
+    // admission reserved room for every resident request's items
+    const int n = std::min((int)lists[b].size(), s->work_cap[b]);
     s->h_nwork[b] = n;
     if (n) {
       std::memcpy(s->h_work[b], lists[b].data(), sizeof(WorkItem) * n);
@@ -589,8 +609,20 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
   }
   if (s->h_stage_size < need * sizeof(float)) {
     if (s->h_stage) cudaFreeHost(s->h_stage);
-    cudaMallocHost(&s->h_stage, need * sizeof(float));
-    s->h_stage_size = need * sizeof(float);
+    s->h_stage = nullptr;
+    s->h_stage_size = 0;
+    if (cudaMallocHost(&s->h_stage, need * sizeof(float)) == cudaSuccess)
+      s->h_stage_size = need * sizeof(float);
+    else
+      cudaGetLastError();
+  }
+  // page-locked staging when it could be had, else pageable memory (the same
+  // copies, without overlap)
+  std::vector<float> pageable;
+  float *stage = s->h_stage;
+  if (!stage) {
+    pageable.resize(need);
+    stage = pageable.data();
   }
   for (size_t k = 0; k < done.size(); ++k) {
     const int slot = done[k];
@@ -600,7 +632,7 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
     cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
                     sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
     for (int f = 0; f < 4; ++f)
-      cudaMemcpy2DAsync(s->h_stage + off[k] + (size_t)f * N * N, sizeof(float) * N,
+      cudaMemcpy2DAsync(stage + off[k] + (size_t)f * N * N, sizeof(float) * N,
                         d.U[d.cur] + f * d.plane + 2 * d.pitch + 2, sizeof(float) * d.pitch, sizeof(float) * N, N,
                         cudaMemcpyDeviceToHost, s->stream);
     // mark the device slot free so stale work-list entries are skipped
@@ -635,10 +667,11 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
       r.cons0[f] = sl.cons0[f];
       r.cons1[f] = c1[f] * area;
     }
-    fin.U.assign(s->h_stage + off[k], s->h_stage + off[k] + 4 * (size_t)N * N);
+    fin.U.assign(stage + off[k], stage + off[k] + 4 * (size_t)N * N);
     fin.gamma = p.gamma0;
     r.done_s = t_done;
     s->arena.release(sl.mem, sl.bytes);
+    s->items_in[sl.bucket] -= d.ntx * d.nty;
     sl.used = false;
     sl.mem = nullptr;
     s->free_slots.push_back(slot);
@@ -800,6 +833,7 @@ void autotune(fv2d_server *s) {
         }
       cudaMemcpyAsync(s->d_sims, s->h_up, sizeof(SimDev) * s->max_sims, cudaMemcpyHostToDevice, s->stream);
       s->n_admitted = 0;
+      for (int q = 0; q < kBuckets; ++q) s->items_in[q] = 0;
       s->lists_dirty = true;
     }
     s->bucket_cfg[b] = best_cfg;
