@@ -80,3 +80,39 @@ def test_create_rejects_bad_params_without_gpu(libs):
         with pytest.raises(Fv2dError) as e:
             Simulation(default_params(**bad))
         assert e.value.code == _abi.ERR_INVALID
+
+
+def _header_fields(header, struct):
+    text = open(os.path.join(REPO, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    body = text[text.index(f"typedef struct {struct} {{"):text.index(f"}} {struct};")]
+    fields = []
+    for line in body.splitlines()[1:]:
+        m = re.match(r"\s*(uint32_t|int32_t|double)\s+(.*);", line)
+        if m:
+            fields += [(n.strip(), m.group(1)) for n in m.group(2).split(",")]
+    return fields
+
+
+def test_server_config_layout_matches_header(libs):
+    from fv2d_gb300.serve import ServerConfig
+    ctypes_of = {"uint32_t": C.c_uint32, "int32_t": C.c_int32, "double": C.c_double}
+    fields = _header_fields("fv2d_serve.h", "fv2d_server_config")
+    assert [(n, ctypes_of[t]) for n, t in fields] == list(ServerConfig._fields_)
+
+
+def test_server_rejects_bad_configs_without_gpu(libs):
+    """Checked before any CUDA call: size, table capacity, budget, scheduling cap."""
+    from fv2d_gb300.serve import ServerConfig, _bind
+    lib = _bind(libs)
+    good = dict(device=0, budget_bytes=1e9, max_sims=16, autotune=0, steps_per_replay=0, tile_config=0,
+                active_cells=0.0)
+    for bad in (dict(max_sims=0), dict(max_sims=1 << 20), dict(budget_bytes=0.0), dict(active_cells=-1.0),
+                dict(active_cells=float("nan")), dict(active_cells=float("inf"))):
+        kw = dict(good, **bad)
+        cfg = ServerConfig(C.sizeof(ServerConfig), **kw)
+        h = C.c_void_p()
+        assert lib.fv2d_server_create(C.byref(cfg), C.byref(h)) == _abi.ERR_INVALID, bad
+    cfg = ServerConfig(C.sizeof(ServerConfig) - 8, **good)
+    h = C.c_void_p()
+    assert lib.fv2d_server_create(C.byref(cfg), C.byref(h)) == _abi.ERR_INVALID
