@@ -37,7 +37,12 @@ static const BatchCfg kCfgs[] = {
     FV2D_MARCH(32, 64, 8, "28x32/64/march"),
     FV2D_MARCH(64, 64, 8, "28x64/64/march"),
     FV2D_MARCH(64, 96, 5, "28x64/96/march"),
+    FV2D_MARCH(16, 64, 8, "28x16/64/march"),
+    FV2D_MARCH(16, 128, 4, "28x16/128/march"),
 };
+
+// the service sizes its per-configuration tables for at most 32 entries
+static_assert(sizeof(kCfgs) / sizeof(kCfgs[0]) <= 32, "more tile configurations than the service's tables hold");
 
 int batch_num_cfgs() { return (int)(sizeof(kCfgs) / sizeof(kCfgs[0])); }
 

@@ -47,6 +47,8 @@ using namespace fv2d;
 namespace {
 
 constexpr int kBuckets = 4;
+constexpr int kMaxCfgs = 32;  // capacity of the per-configuration tables (batch_kernels.cu asserts the bound)
+int num_cfgs() { return std::min(batch_num_cfgs(), kMaxCfgs); }
 constexpr int kConsBlocks = 64;
 
 int bucket_of(int N) { return N < 128 ? 0 : (N < 256 ? 1 : (N < 512 ? 2 : 3)); }
@@ -265,7 +267,7 @@ struct fv2d_server {
   int work_cap[kBuckets] = {};
   int items_in[kBuckets] = {};  // work items of the resident requests, per bucket
   int bucket_cfg[kBuckets] = {1, 2, 3, 3};
-  int cfg_grid[16] = {};
+  int cfg_grid[kMaxCfgs] = {};
   bool lists_dirty = true;
   int mask = 0;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (K, bucket mask) -> graph
@@ -781,7 +783,7 @@ void worker_main(fv2d_server *s) {
 // fastest.
 void autotune(fv2d_server *s) {
   const int rep[kBuckets] = {96, 192, 384, 768};
-  const int ncfg = batch_num_cfgs();
+  const int ncfg = num_cfgs();
   for (int b = 0; b < kBuckets; ++b) {
     const int N = rep[b];
     const int nsims = std::max(2, std::min(256, (int)(24e6 / ((double)N * N))));
@@ -897,11 +899,11 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   cudaMemcpy(s->d_nwork, s->h_nwork, sizeof(int) * kBuckets, cudaMemcpyHostToDevice);
   s->slots.resize(s->max_sims);
   for (int k = s->max_sims - 1; k >= 0; --k) s->free_slots.push_back(k);
-  for (int c = 0; c < batch_num_cfgs(); ++c) {
+  for (int c = 0; c < num_cfgs(); ++c) {
     int per_sm = 0;
     if (batch_setup(c, &per_sm) == cudaSuccess && per_sm > 0) s->cfg_grid[c] = per_sm * s->num_sms;
   }
-  if (cfg->tile_config > 0 && cfg->tile_config <= batch_num_cfgs() && s->cfg_grid[cfg->tile_config - 1]) {
+  if (cfg->tile_config > 0 && cfg->tile_config <= num_cfgs() && s->cfg_grid[cfg->tile_config - 1]) {
     for (int b = 0; b < kBuckets; ++b) s->bucket_cfg[b] = cfg->tile_config - 1;
   } else if (cfg->autotune) {
     autotune(s);
