@@ -285,8 +285,15 @@ struct fv2d_server {
   int64_t n_submitted = 0, n_admitted = 0, n_completed = 0, n_failed = 0;
   std::atomic<bool> stop{false};
   std::thread worker;
-  double cell_updates = 0, busy_s = 0;
+  double cell_updates = 0, busy_s = 0;  // written by the worker; published below under mu
   int replays = 0;
+  int n_active = 0;  // resident requests (worker only)
+  // copies for fv2d_server_get_stats, updated under mu
+  struct Published {
+    double cell_updates = 0, busy_s = 0, bytes_in_use = 0, bytes_reserved = 0;
+    int replays = 0, active = 0;
+    int64_t admitted = 0;
+  } pub;
   double rate_est = 2e10;  // cell-updates/s, refined by measurement
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // the buckets' step chains run as parallel branches of a replay graph
@@ -464,6 +471,7 @@ int admit(fv2d_server *s, const Pending &pd) {
   if (pd.id > 0)  // the autotuner's synthetic states need no sums
     cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
   s->n_admitted++;
+  s->n_active++;
   s->lists_dirty = true;
   return slot;
 }
@@ -496,6 +504,17 @@ void read_initial_cons(fv2d_server *s, const std::vector<int> &fresh) {
     sum_cons(s->h_cons + (size_t)slot * kConsBlocks * 8, sl.cons0);
     for (int f = 0; f < 4; ++f) sl.cons0[f] *= area;
   }
+}
+
+// Copy the worker's counters for fv2d_server_get_stats; the caller holds mu.
+void publish_locked(fv2d_server *s) {
+  s->pub.cell_updates = s->cell_updates;
+  s->pub.busy_s = s->busy_s;
+  s->pub.replays = s->replays;
+  s->pub.admitted = s->n_admitted;
+  s->pub.active = s->n_active;
+  s->pub.bytes_in_use = (double)s->arena.in_use;
+  s->pub.bytes_reserved = (double)s->arena.reserved;
 }
 
 // Remaining cell-updates of a resident request: its remaining steps (the
@@ -674,11 +693,13 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
     r.done_s = t_done;
     s->arena.release(sl.mem, sl.bytes);
     s->items_in[sl.bucket] -= d.ntx * d.nty;
+    s->n_active--;
     sl.used = false;
     sl.mem = nullptr;
     s->free_slots.push_back(slot);
     s->lists_dirty = true;
     std::lock_guard<std::mutex> lock(s->mu);
+    publish_locked(s);  // before the completion count that fv2d_server_drain waits for
     if (r.status == FV2D_OK)
       s->n_completed++;
     else
@@ -738,6 +759,8 @@ bool run_once(fv2d_server *s, int K_fixed) {
   s->cell_updates += cells;
   if (ms > 0.05 && cells > 0) s->rate_est = 0.5 * s->rate_est + 0.5 * (cells / (ms * 1e-3));
   retire_all(s, done);
+  std::lock_guard<std::mutex> lock(s->mu);
+  publish_locked(s);
   return true;
 }
 
@@ -774,6 +797,10 @@ void worker_main(fv2d_server *s) {
       for (auto it = keep.rbegin(); it != keep.rend(); ++it) s->queue.push_front(*it);
     }
     read_initial_cons(s, fresh);
+    if (!fresh.empty()) {
+      std::lock_guard<std::mutex> lock(s->mu);
+      publish_locked(s);
+    }
     run_once(s, s->cfg.steps_per_replay);
   }
 }
@@ -835,6 +862,7 @@ void autotune(fv2d_server *s) {
         }
       cudaMemcpyAsync(s->d_sims, s->h_up, sizeof(SimDev) * s->max_sims, cudaMemcpyHostToDevice, s->stream);
       s->n_admitted = 0;
+      s->n_active = 0;
       for (int q = 0; q < kBuckets; ++q) s->items_in[q] = 0;
       s->lists_dirty = true;
     }
@@ -908,6 +936,7 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   } else if (cfg->autotune) {
     autotune(s);
   }
+  publish_locked(s);  // no other thread yet
   s->worker = std::thread(worker_main, s);
   *out = s;
   return FV2D_OK;
@@ -1017,20 +1046,19 @@ int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out) {
   if (!s || !out) return FV2D_ERR_INVALID;
   std::lock_guard<std::mutex> lock(s->mu);
   std::memset(out, 0, sizeof(*out));
+  // counters of the worker thread as it last published them
   out->submitted = s->n_submitted;
-  out->admitted = s->n_admitted;
+  out->admitted = s->pub.admitted;
   out->completed = s->n_completed;
   out->failed = s->n_failed;
-  int active = 0;
-  for (auto &sl : s->slots) active += sl.used;
-  out->active = active;
+  out->active = s->pub.active;
   out->queued = (int)s->queue.size();
-  out->cell_updates = s->cell_updates;
-  out->busy_s = s->busy_s;
-  out->bytes_in_use = (double)s->arena.in_use;
-  out->bytes_reserved = (double)s->arena.reserved;
+  out->cell_updates = s->pub.cell_updates;
+  out->busy_s = s->pub.busy_s;
+  out->bytes_in_use = s->pub.bytes_in_use;
+  out->bytes_reserved = s->pub.bytes_reserved;
   for (int b = 0; b < kBuckets; ++b) out->bucket_cfg[b] = s->bucket_cfg[b];
-  out->replays = s->replays;
+  out->replays = s->pub.replays;
   return FV2D_OK;
 }
 
