@@ -82,7 +82,11 @@ int fv2d_set_host_mirror(fv2d_ctx *ctx, double *q_host);
 /* Interior conservative state (rho, rho u, rho v, E). */
 int fv2d_get_cons(fv2d_ctx *ctx, double *u_host);
 
-/* Same as set_prim / get_prim with device-resident interleaved arrays. */
+/* Same as set_prim / get_prim with device-resident interleaved arrays.
+ * set_prim_device is ordered on the context's stream and returns before the
+ * copy has run: q_dev must not change until work on that stream after the
+ * call (or a synchronisation) has completed.  get_prim_device returns with the
+ * copy complete. */
 int fv2d_set_prim_device(fv2d_ctx *ctx, const double *q_dev);
 int fv2d_get_prim_device(fv2d_ctx *ctx, double *q_dev);
 
