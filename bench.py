@@ -614,7 +614,7 @@ def main():
                      "traffic": (traffic * cells) if traffic else None, "peak_kind": peak_kind,
                      "bytes_per_cell": BYTES_PER_CELL, "kernel": "fv2d::step_kernel<PLM,HLLC>",
                      "duration": "CUDA events per iteration: the step kernel plus its one-thread commit kernel "
-                                 "(~4.6 us, 0.3 % of the iteration in the ncu launch list)",
+                                 "(~4.7 us, 0.4 % of the iteration in the ncu launch list)",
                      "binding": "instruction issue, not HBM: binary64 pipe ~64 %, integer ALU ~55 % busy "
                                 "(profiles/step_fp64_plm_hllc_sedov.txt); see roofline_fp64"},
         "roofline_fp64": fp64,
