@@ -39,6 +39,7 @@ static const BatchCfg kCfgs[] = {
     FV2D_MARCH(64, 96, 5, "28x64/96/march"),
     FV2D_MARCH(16, 64, 8, "28x16/64/march"),
     FV2D_MARCH(16, 128, 4, "28x16/128/march"),
+    FV2D_MARCH(32, 32, 16, "28x32/32/march"),
 };
 
 // the service sizes its per-configuration tables for at most 32 entries
