@@ -137,8 +137,10 @@ struct Smem {
   static constexpr size_t BYTES = sizeof(double) * (TOTAL + 1) + 128;  // + spare slot + alignment slack
 };
 
+// 3 CTAs per SM; PLM + HLL without viscosity measured faster at 4 (56
+// registers with some spills; its shared memory still fits four times).
 template <int RECON, int RS, bool VISC>
-__global__ void __launch_bounds__(NT, 3)
+__global__ void __launch_bounds__(NT, (RECON == RECON_PLM && RS == RS_HLL && !VISC) ? 4 : 3)
     step_kernel(const __grid_constant__ CUtensorMap tmQ0, const __grid_constant__ CUtensorMap tmQ1,
                 const StepArgs a) {
   using L = Smem<RECON, VISC>;
