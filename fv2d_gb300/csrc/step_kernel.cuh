@@ -137,10 +137,20 @@ struct Smem {
   static constexpr size_t BYTES = sizeof(double) * (TOTAL + 1) + 128;  // + spare slot + alignment slack
 };
 
-// 3 CTAs per SM; PLM + HLL without viscosity measured faster at 4 (56
-// registers with some spills; its shared memory still fits four times).
+// CTAs per SM: 3.  Without viscosity, measured faster with more at the price
+// of register spills (their shared memory still fits): PCM with HLL or HLLC
+// at 5 (40 registers), PCM with FSLP and PLM with HLL or FSLP at 4 (56); PLM
+// and MUSCL-Hancock with HLLC stay at 3.
+template <int RECON, int RS>
+constexpr int step_ctas_per_sm(bool visc) {
+  if (visc) return 3;
+  if (RECON == RECON_PCM) return RS == RS_FSLP ? 4 : 5;
+  if (RECON == RECON_PLM && RS != RS_HLLC) return 4;
+  return 3;
+}
+
 template <int RECON, int RS, bool VISC>
-__global__ void __launch_bounds__(NT, (RECON == RECON_PLM && RS == RS_HLL && !VISC) ? 4 : 3)
+__global__ void __launch_bounds__(NT, step_ctas_per_sm<RECON, RS>(VISC))
     step_kernel(const __grid_constant__ CUtensorMap tmQ0, const __grid_constant__ CUtensorMap tmQ1,
                 const StepArgs a) {
   using L = Smem<RECON, VISC>;
