@@ -40,6 +40,8 @@ static const BatchCfg kCfgs[] = {
     FV2D_MARCH(16, 64, 8, "28x16/64/march"),
     FV2D_MARCH(16, 128, 4, "28x16/128/march"),
     FV2D_MARCH(32, 32, 16, "28x32/32/march"),
+    FV2D_MARCH(32, 64, 10, "28x32/64x10/march"),
+    FV2D_MARCH(32, 32, 20, "28x32/32x20/march"),
 };
 
 // the service sizes its per-configuration tables for at most 32 entries
