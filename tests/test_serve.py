@@ -142,3 +142,46 @@ def test_rejects_unsupported_requests(gpu_lib):
                 s.submit("sedov", params(128, **bad), 10)
         with pytest.raises(ValueError):
             s.submit("sedov", params(100), 10)  # not a multiple of 32
+
+
+@pytest.mark.parametrize("active", [0.0, 2e5])
+def test_many_small_requests(gpu_lib, active):
+    """400 requests submitted at once: the work lists grow while requests are
+    admitted, every request completes with its own step count, all state
+    memory is returned, and a sample matches its stand-alone result."""
+    import fv2d_gb300 as fv
+    from fv2d_gb300.serve import Server
+    rng = np.random.default_rng(17)
+    reqs = []
+    for k in range(400):
+        N = int(rng.choice([64, 96, 128, 160]))
+        kind = k % 3
+        if kind == 0:
+            reqs.append(("sedov", params(N), int(rng.integers(5, 25))))
+        elif kind == 1:
+            reqs.append(("sod_x", params(N, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC),
+                         int(rng.integers(5, 25))))
+        else:
+            reqs.append(("kh_step", params(N, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC, seed=k),
+                         int(rng.integers(5, 25))))
+    sample = [0, 1, 2, 199, 398, 399]
+    alone = {}
+    with Server(budget_bytes=4e9, autotune=False) as s:
+        for k in sample:
+            rid = s.submit(*reqs[k])
+            assert s.drain(60) == 0
+            res = {r.id: r for r in s.poll()}
+            alone[k] = s.get_prim(rid)
+    with Server(budget_bytes=4e9, autotune=False, active_cells=active) as s:
+        ids = [s.submit(*r) for r in reqs]
+        assert s.drain(300) == 0
+        res = {r.id: r for r in s.poll()}
+        assert len(res) == len(reqs)
+        for k, rid in enumerate(ids):
+            assert res[rid].status == 0 and res[rid].steps == reqs[k][2], k
+        for k in sample:
+            assert bits_equal(s.get_prim(ids[k]), alone[k]), k
+        for rid in ids:
+            s.release(rid)
+        st = s.stats()
+        assert st.active == 0 and st.completed == len(reqs) and st.bytes_in_use == 0
