@@ -175,22 +175,27 @@ class Simulation:
         self.close()
 
     def set_stream(self, stream_ptr):
+        """Queue the context's work on a caller's CUDA stream (0: its own)."""
         self._check(self._lib.fv2d_set_stream(self.h, C.c_void_p(stream_ptr)))
 
     def init_problem(self, name):
+        """InitFunctor::init + primToCons (Init.h:310-358) for a problem name or id."""
         pb = PROBLEMS[name] if isinstance(name, str) else int(name)
         self._check(self._lib.fv2d_init_problem(self.h, pb))
 
     def set_prim(self, q):
+        """Replace the state by the interior primitives q (Ny, Nx, 4) = rho, u, v, p."""
         q = np.ascontiguousarray(q, dtype=np.float64)
         if q.shape != (self.ny, self.nx, 4):
             raise ValueError(f"expected shape {(self.ny, self.nx, 4)}, got {q.shape}")
         self._check(self._lib.fv2d_set_prim(self.h, _ptr(q)))
 
     def set_prim_ptr(self, host_ptr):
+        """set_prim from a host address (page-locked memory is read by the device directly)."""
         self._check(self._lib.fv2d_set_prim(self.h, C.cast(C.c_void_p(host_ptr), _dp)))
 
     def get_prim_ptr(self, host_ptr):
+        """get_prim into a host address (the registered host mirror is returned without a copy)."""
         self._check(self._lib.fv2d_get_prim(self.h, C.cast(C.c_void_p(host_ptr), _dp)))
 
     def set_host_mirror(self, host_ptr):
@@ -199,17 +204,21 @@ class Simulation:
         self._check(self._lib.fv2d_set_host_mirror(self.h, C.c_void_p(host_ptr) if host_ptr else None))
 
     def set_prim_device(self, dev_ptr):
+        """set_prim from a device array, ordered on the context's stream."""
         self._check(self._lib.fv2d_set_prim_device(self.h, C.c_void_p(dev_ptr)))
 
     def get_prim_device(self, dev_ptr):
+        """get_prim into a device array (complete on return)."""
         self._check(self._lib.fv2d_get_prim_device(self.h, C.c_void_p(dev_ptr)))
 
     def get_prim(self):
+        """Interior primitives (Ny, Nx, 4) = rho, u, v, p after the last update."""
         q = np.empty((self.ny, self.nx, 4))
         self._check(self._lib.fv2d_get_prim(self.h, _ptr(q)))
         return q
 
     def get_cons(self):
+        """Interior conservative state (Ny, Nx, 4) = rho, rho u, rho v, E."""
         u = np.empty((self.ny, self.nx, 4))
         self._check(self._lib.fv2d_get_cons(self.h, _ptr(u)))
         return u
@@ -232,6 +241,7 @@ class Simulation:
         return v.value
 
     def counters(self):
+        """checkNegatives counts (SimInfo.h:637-645): negative density, negative pressure, NaN."""
         c = (C.c_uint64 * 3)()
         self._check(self._lib.fv2d_get_counters(self.h, c))
         return list(c)
@@ -252,12 +262,14 @@ class Simulation:
         self._check(self._lib.fv2d_run_async(self.h, int(n)))
 
     def time(self):
+        """(t, iteration) of the device-driven clock."""
         t = C.c_double()
         it = C.c_int()
         self._check(self._lib.fv2d_get_time(self.h, C.byref(t), C.byref(it)))
         return t.value, it.value
 
     def set_time(self, t, iteration):
+        """Set the device-driven clock (a restart sets the snapshot's time and iteration)."""
         self._check(self._lib.fv2d_set_time(self.h, float(t), int(iteration)))
 
     def step_log(self, max_records=4096):
