@@ -241,7 +241,9 @@ class Simulation:
         return v.value
 
     def counters(self):
-        """checkNegatives counts (SimInfo.h:637-645): negative density, negative pressure, NaN."""
+        """checkNegatives counts (SimInfo.h:602-645): negative densities, negative pressures and
+        NaN values (each field of each interior cell counted).
+        """
         c = (C.c_uint64 * 3)()
         self._check(self._lib.fv2d_get_counters(self.h, c))
         return list(c)
