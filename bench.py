@@ -139,9 +139,10 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_oracle_rate(n, steps_cap=20, budget_s=15.0):
+def cpu_oracle_rate(n, steps_cap=500, budget_s=12.0):
     """Oracle (OpenMP over all host cores) cell-updates/s on a bounded sample
-    of the workload: the same Sedov grid, as many iterations as fit ~budget."""
+    of the workload: the same Sedov grid, as many iterations as fit about
+    budget_s seconds (at most steps_cap)."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
     import fv2d_testlib as T
     lib = T.oracle_lib()
