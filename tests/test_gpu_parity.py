@@ -217,6 +217,45 @@ def test_full_size_sedov_matches_oracle(gpu_lib):
     assert bits_equal(s2.get_cons(), u1)
 
 
+FULL_SIZE = {
+    # KH 4096^2, CFL 0.7, periodic: mass, both momenta and energy are conserved
+    "kh_4096": ("kh_step", dict(Nx=4096, Ny=4096, gamma0=1.4, reconstruction=2, riemann_solver=1, CFL=0.7,
+                                boundary_x=2, boundary_y=2), (0, 1, 2, 3)),
+    # RT 1024x3072 (HLL, gravity, conduction, viscosity), periodic in x, reflecting in y: mass is conserved
+    "rt_1024x3072": ("rt_hydrostatic", dict(Nx=1024, Ny=3072, xmax=0.5, ymax=1.5, gamma0=1.4, reconstruction=2,
+                                            riemann_solver=0, CFL=0.8, boundary_x=2, boundary_y=1, gravity_mode=1,
+                                            gy=-0.1, thermal_conductivity_active=1, kappa=1e-4,
+                                            viscosity_active=1, mu=1e-4), (0,)),
+}
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("case", sorted(FULL_SIZE))
+def test_full_size_kh_and_rt_match_oracle(gpu_lib, case):
+    """The other two benchmark set-ups at their full sizes: bitwise against
+    the oracle for 3 iterations, then the conserved sums over 20 more."""
+    problem, kw, conserved = FULL_SIZE[case]
+    p = reference_params(**kw)
+    o, s = Oracle(p), gpu_sim(p)
+    o.init_problem(problem)
+    s.init_problem(problem)
+    for _ in range(3):
+        d = o.compute_dt()
+        assert bits_equal(s.compute_dt()[0], d[0])
+        o.update(d[0])
+        s.update(d[0])
+    assert bits_equal(s.get_prim(), o.get_prim())
+    assert o.counters() == s.counters()
+    del o
+    u0 = s.get_cons()
+    s.advance(20, 1e9)
+    u1 = s.get_cons()
+    for k in conserved:
+        a, b = np.sum(u0[..., k], dtype=np.float64), np.sum(u1[..., k], dtype=np.float64)
+        scale = np.sum(np.abs(u0[..., k]), dtype=np.float64)
+        assert abs(b - a) <= 1e-10 * scale, (k, a, b)
+
+
 def test_page_locked_input_and_host_mirror_match_pageable_path(gpu_lib):
     """set_prim from page-locked memory (read by the set-up kernel over the
     host link) and the host mirror written by the step kernel give the same
