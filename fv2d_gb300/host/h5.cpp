@@ -418,6 +418,7 @@ bool write_unique(const std::string &path, bool truncate, const RootInfo &root, 
     return fail("unexpected root group structure in " + path);
   const uint64_t snod = rd(tb + 32, 8);
   const uint64_t heap_size = rd(hh + 8, 8), heap_data = rd(hh + 24, 8);
+  if (heap_size > ROOT_HEAP_CAP) return fail("unexpected root group structure in " + path);
   std::vector<uint8_t> heap(heap_size), sn(SNOD_SIZE);
   if (!w.get(heap_data, heap.data(), heap_size) || !w.get(snod, sn.data(), SNOD_SIZE) ||
       std::memcmp(sn.data(), "SNOD", 4) != 0)
@@ -429,7 +430,10 @@ bool write_unique(const std::string &path, bool truncate, const RootInfo &root, 
   for (int k = 0; k < nsym; ++k) {
     const uint8_t *e = sn.data() + 8 + 40 * k;
     Writer::Entry en;
-    en.name = std::string((const char *)heap.data() + rd(e, 8));
+    const uint64_t noff = rd(e, 8);
+    const void *z = noff < heap_size ? std::memchr(heap.data() + noff, 0, heap_size - noff) : nullptr;
+    if (!z) return fail("unexpected root group structure in " + path);
+    en.name = std::string((const char *)heap.data() + noff, (const char *)z - (const char *)heap.data() - noff);
     en.oh = rd(e + 8, 8);
     en.group = rd(e + 16, 4) == 1;
     en.btree = rd(e + 24, 8);
@@ -582,21 +586,41 @@ struct Msg {
   std::vector<uint8_t> data;
 };
 
+// Bounds-checked little-endian field of a message payload.
+bool field(const std::vector<uint8_t> &v, size_t off, int n, uint64_t *out) {
+  if (n < 0 || n > 8 || off > v.size() || (size_t)n > v.size() - off) return false;
+  *out = rd(v.data() + off, n);
+  return true;
+}
+
+// The reader treats every size, offset and count in the file as untrusted:
+// reads stay inside the file, payload fields inside their message, and the
+// walks over header continuations and group B-trees are bounded.
+constexpr size_t kMaxHeaderChunks = 1024;
+constexpr int kMaxTreeDepth = 32;
+constexpr size_t kMaxTreeNodes = 1 << 16;
+
 struct File::Impl {
   std::ifstream in;
-  uint64_t base = 0;
+  uint64_t base = 0, file_size = 0;
   int so = 8, sl = 8;
   uint64_t root_oh = UNDEF;
 
+  bool inside(uint64_t addr, uint64_t n) const {
+    return addr <= file_size && base <= file_size - addr && n <= file_size - addr - base;
+  }
   bool read(uint64_t addr, void *p, size_t n) {
+    if (!inside(addr, n)) return false;
     in.clear();
     in.seekg((std::streamoff)(base + addr));
     in.read((char *)p, (std::streamsize)n);
     return (size_t)in.gcount() == n;
   }
-  std::vector<uint8_t> read(uint64_t addr, size_t n) {
-    std::vector<uint8_t> v(n);
-    if (!read(addr, v.data(), n)) v.clear();
+  std::vector<uint8_t> read(uint64_t addr, uint64_t n) {
+    std::vector<uint8_t> v;
+    if (!inside(addr, n)) return v;  // never allocate more than the file holds
+    v.resize((size_t)n);
+    if (!read(addr, v.data(), (size_t)n)) v.clear();
     return v;
   }
 
@@ -608,18 +632,22 @@ struct File::Impl {
       std::vector<std::pair<uint64_t, uint64_t>> chunks{{addr + 16, rd(pre + 8, 4)}};
       int seen = 0;
       for (size_t c = 0; c < chunks.size() && seen < nmsgs; ++c) {
+        if (c >= kMaxHeaderChunks) return false;
         std::vector<uint8_t> b = read(chunks[c].first, chunks[c].second);
         if (b.size() != chunks[c].second) return false;
         size_t p = 0;
         while (p + 8 <= b.size() && seen < nmsgs) {
           const int type = (int)rd(&b[p], 2);
           const size_t sz = rd(&b[p + 2], 2);
-          if (p + 8 + sz > b.size()) return false;
+          if (sz > b.size() - p - 8) return false;
           std::vector<uint8_t> d(b.begin() + p + 8, b.begin() + p + 8 + sz);
-          if (type == 0x0010)
-            chunks.push_back({rd(d.data(), so), rd(d.data() + so, sl)});
-          else
+          if (type == 0x0010) {
+            uint64_t at, len;
+            if (!field(d, 0, so, &at) || !field(d, so, sl, &len)) return false;
+            chunks.push_back({at, len});
+          } else {
             out->push_back({type, std::move(d)});
+          }
           p += 8 + sz;
           ++seen;
         }
@@ -638,20 +666,25 @@ struct File::Impl {
       p += szlen;
       std::vector<std::pair<uint64_t, uint64_t>> chunks{{addr + p, chunk0}};
       for (size_t c = 0; c < chunks.size(); ++c) {
+        if (c >= kMaxHeaderChunks) return false;
         std::vector<uint8_t> b = read(chunks[c].first, chunks[c].second);
         if (b.size() != chunks[c].second) return false;
+        if (c > 0 && b.size() < 4) return false;
         size_t q = (c == 0) ? 0 : 4;  // continuation chunks start with "OCHK"
         const size_t end = b.size() - (c == 0 ? 0 : 4);
         const size_t hdr = 4 + ((flags & 0x04) ? 2 : 0);
         while (q + hdr <= end) {
           const int type = b[q];
           const size_t sz = rd(&b[q + 1], 2);
-          if (q + hdr + sz > end) break;
+          if (sz > end - q - hdr) break;
           std::vector<uint8_t> d(b.begin() + q + hdr, b.begin() + q + hdr + sz);
-          if (type == 0x10)
-            chunks.push_back({rd(d.data(), so), rd(d.data() + so, sl)});
-          else if (type != 0)
+          if (type == 0x10) {
+            uint64_t at, len;
+            if (!field(d, 0, so, &at) || !field(d, so, sl, &len)) return false;
+            chunks.push_back({at, len});
+          } else if (type != 0) {
             out->push_back({type, std::move(d)});
+          }
           q += hdr + sz;
         }
       }
@@ -668,52 +701,66 @@ struct File::Impl {
     for (auto &m : ms) {
       if (m.type == 0x0011) {  // symbol table
         found = true;
-        const uint64_t btree = rd(m.data.data(), so), heap = rd(m.data.data() + so, so);
+        uint64_t btree, heap;
+        if (!field(m.data, 0, so, &btree) || !field(m.data, so, so, &heap)) return false;
         uint8_t hh[64];
         if (!read(heap, hh, 8 + 2 * sl + so) || std::memcmp(hh, "HEAP", 4) != 0) return false;
         const uint64_t hsize = rd(hh + 8, sl), hdata = rd(hh + 8 + 2 * sl, so);
         std::vector<uint8_t> names = read(hdata, hsize);
         if (names.size() != hsize) return false;
-        std::function<bool(uint64_t)> walk = [&](uint64_t node) -> bool {
+        size_t visited = 0;
+        std::function<bool(uint64_t, int)> walk = [&](uint64_t node, int depth) -> bool {
+          if (depth > kMaxTreeDepth || ++visited > kMaxTreeNodes) return false;
           uint8_t th[8];
           if (!read(node, th, 8) || std::memcmp(th, "TREE", 4) != 0) return false;
           const int level = th[5], used = (int)rd(th + 6, 2);
-          const std::vector<uint8_t> body = read(node + 8 + 2 * so, (size_t)used * (so + sl) + sl);
+          const std::vector<uint8_t> body = read(node + 8 + 2 * so, (uint64_t)used * (so + sl) + sl);
           if (body.empty()) return false;
           for (int k = 0; k < used; ++k) {
             const uint64_t child = rd(body.data() + sl + (size_t)k * (so + sl), so);
             if (level > 0) {
-              if (!walk(child)) return false;
+              if (!walk(child, depth + 1)) return false;
               continue;
             }
             uint8_t sh[8];
             if (!read(child, sh, 8) || std::memcmp(sh, "SNOD", 4) != 0) return false;
             const int ns = (int)rd(sh + 6, 2);
             const size_t esz = 2 * so + 4 + 4 + 16;
-            const std::vector<uint8_t> es = read(child + 8, ns * esz);
+            const std::vector<uint8_t> es = read(child + 8, (uint64_t)ns * esz);
+            if (es.size() != (size_t)ns * esz) return false;
             for (int e = 0; e < ns; ++e) {
               const uint64_t noff = rd(es.data() + e * esz, so);
               if (noff >= names.size()) return false;
-              (*out)[std::string((const char *)names.data() + noff)] = rd(es.data() + e * esz + so, so);
+              const char *nm = (const char *)names.data() + noff;
+              const void *z = std::memchr(nm, 0, names.size() - noff);
+              if (!z) return false;  // a name must end inside the heap
+              (*out)[std::string(nm, (const char *)z - nm)] = rd(es.data() + e * esz + so, so);
             }
           }
           return true;
         };
-        if (!walk(btree)) return false;
+        if (!walk(btree, 0)) return false;
       } else if (m.type == 0x0006) {  // link message (compact new-style groups)
-        const uint8_t *d = m.data.data();
-        const int fl = d[1];
+        const std::vector<uint8_t> &d = m.data;
+        uint64_t fl, ltype = 0, nlen, addr;
+        if (!field(d, 1, 1, &fl)) return false;
         size_t p = 2;
-        int ltype = 0;
-        if (fl & 0x08) ltype = d[p++];
+        if (fl & 0x08) {
+          if (!field(d, p, 1, &ltype)) return false;
+          ++p;
+        }
         if (fl & 0x04) p += 8;
         if (fl & 0x10) p += 1;
         const int lsz = 1 << (fl & 3);
-        const size_t nlen = rd(d + p, lsz);
+        if (!field(d, p, lsz, &nlen)) return false;
         p += lsz;
-        const std::string name((const char *)d + p, nlen);
-        p += nlen;
-        if (ltype == 0) (*out)[name] = rd(d + p, so);
+        if (p > d.size() || nlen > d.size() - p) return false;
+        const std::string name((const char *)d.data() + p, (size_t)nlen);
+        p += (size_t)nlen;
+        if (ltype == 0) {
+          if (!field(d, p, so, &addr)) return false;
+          (*out)[name] = addr;
+        }
         found = true;
       } else if (m.type == 0x0002) {
         found = true;  // link info: dense storage is not read here
@@ -753,29 +800,41 @@ struct File::Impl {
     if (!header(oh, &ms)) return false;
     for (auto &m : ms) {
       if (m.type != 0x000C) continue;
-      const uint8_t *d = m.data.data();
-      const int ver = d[0];
-      const size_t nsz = rd(d + 2, 2), dtsz = rd(d + 4, 2), dssz = rd(d + 6, 2);
+      const std::vector<uint8_t> &v = m.data;
+      uint64_t ver, nsz, dtsz, dssz;
+      if (!field(v, 0, 1, &ver) || !field(v, 2, 2, &nsz) || !field(v, 4, 2, &dtsz) || !field(v, 6, 2, &dssz))
+        return false;
       size_t p = 8 + (ver == 3 ? 1 : 0);
-      auto adv = [&](size_t n) { return ver == 1 ? align8(n) : n; };
-      const std::string an((const char *)d + p, nsz ? nsz - 1 : 0);
+      auto adv = [&](uint64_t n) { return ver == 1 ? align8(n) : n; };
+      if (p > v.size() || nsz > v.size() - p) return false;
+      const std::string an((const char *)v.data() + p, nsz ? (size_t)nsz - 1 : 0);
       p += adv(nsz);
-      const uint8_t *dt = d + p;
+      const size_t dt = p;
       p += adv(dtsz);
-      const uint8_t *ds = d + p;
+      const size_t ds = p;
       p += adv(dssz);
       if (an != name) continue;
-      a->dclass = dt[0] & 0x0f;
-      a->dsize = (int)rd(dt + 4, 4);
-      a->is_signed = (dt[1] & 0x08) != 0;
-      const int dver = ds[0], rank = ds[1];
+      uint64_t c0, c1, dsize, dver, rank, dstype = 0;
+      if (!field(v, dt, 1, &c0) || !field(v, dt + 1, 1, &c1) || !field(v, dt + 4, 4, &dsize)) return false;
+      if (!field(v, ds, 1, &dver) || !field(v, ds + 1, 1, &rank)) return false;
+      if (dver == 2 && !field(v, ds + 3, 1, &dstype)) return false;
+      if (dsize == 0 || dsize > 1024) return false;
+      a->dclass = (int)(c0 & 0x0f);
+      a->dsize = (int)dsize;
+      a->is_signed = (c1 & 0x08) != 0;
       const size_t dp = (dver == 1) ? 8 : 4;
       a->nelem = 1;
-      for (int k = 0; k < rank; ++k) a->nelem *= rd(ds + dp + 8 * k, 8);
-      if (dver == 2 && ds[3] == 2) a->nelem = 0;  // null dataspace
+      for (uint64_t k = 0; k < rank; ++k) {
+        uint64_t e;
+        if (!field(v, ds + dp + 8 * k, 8, &e)) return false;
+        if (e != 0 && a->nelem > (v.size() / e)) return false;  // more elements than the message holds
+        a->nelem *= e;
+      }
+      if (dver == 2 && dstype == 2) a->nelem = 0;  // null dataspace
+      if (a->nelem > v.size() / (uint64_t)a->dsize) return false;
       const size_t nb = (size_t)a->nelem * a->dsize;
-      if (p + nb > m.data.size()) return false;
-      a->data.assign(d + p, d + p + nb);
+      if (p > v.size() || nb > v.size() - p) return false;
+      a->data.assign(v.data() + p, v.data() + p + nb);
       return true;
     }
     return false;
@@ -790,6 +849,9 @@ bool File::open(const std::string &path, std::string *err) {
     if (err) *err = "cannot open " + path;
     return false;
   }
+  I.in.seekg(0, std::ios::end);
+  const std::streamoff fsz = I.in.tellg();
+  I.file_size = fsz > 0 ? (uint64_t)fsz : 0;
   // the superblock sits at 0 or after a user block of 512, 1024, 2048, ... bytes
   uint64_t at = 0;
   uint8_t sb[128];
@@ -802,30 +864,42 @@ bool File::open(const std::string &path, std::string *err) {
     if (std::memcmp(sb, SIGNATURE, 8) == 0) break;
     at = at ? at * 2 : 512;
   }
-  if (!I.read(at, sb, sizeof sb)) {
+  std::memset(sb, 0, sizeof sb);
+  if (!I.read(at, sb, std::min<uint64_t>(sizeof sb, I.file_size - at))) {
     if (err) *err = "short superblock in " + path;
     return false;
   }
   const int ver = sb[8];
+  uint64_t base;
   if (ver <= 1) {
     I.so = sb[13];
     I.sl = sb[14];
-    size_t p = 24 + (ver == 1 ? 4 : 0);
-    const uint64_t base = rd(sb + p, I.so);
-    p += 4 * I.so;           // base, free-space, end-of-file, driver info
-    p += I.so;               // root entry: link name offset
-    I.root_oh = rd(sb + p, I.so);
-    I.base = base;
   } else {
     I.so = sb[9];
     I.sl = sb[10];
+  }
+  if ((I.so != 2 && I.so != 4 && I.so != 8) || (I.sl != 2 && I.sl != 4 && I.sl != 8)) {
+    if (err) *err = "unsupported offset or length size in " + path;
+    return false;
+  }
+  if (ver <= 1) {
+    size_t p = 24 + (ver == 1 ? 4 : 0);
+    base = rd(sb + p, I.so);
+    p += 4 * I.so;  // base, free-space, end-of-file, driver info
+    p += I.so;      // root entry: link name offset
+    I.root_oh = rd(sb + p, I.so);
+  } else {
     size_t p = 12;
-    const uint64_t base = rd(sb + p, I.so);
+    base = rd(sb + p, I.so);
     p += 3 * I.so;  // base, superblock extension, end of file
     I.root_oh = rd(sb + p, I.so);
-    I.base = base;
   }
+  I.base = base;
   if (I.base == 0 && at != 0) I.base = at;  // base address relative to the user block
+  if (I.base > I.file_size) {
+    if (err) *err = "base address past the end of " + path;
+    return false;
+  }
   return true;
 }
 
@@ -859,59 +933,70 @@ bool File::read_doubles(const std::string &dataset, std::vector<double> *out, st
   uint64_t addr = UNDEF, size = 0;
   std::vector<uint8_t> compact;
   for (auto &m : ms) {
-    const uint8_t *p = m.data.data();
-    if (m.type == 0x0001) {
-      const int ver = p[0], rank = p[1];
-      const size_t o = ver == 1 ? 8 : 4;
-      for (int k = 0; k < rank; ++k) d.push_back(rd(p + o + 8 * k, sl));
-    } else if (m.type == 0x0003) {
-      dclass = p[0] & 0x0f;
-      big_endian = (p[1] & 1) != 0;
-      dsize = (int)rd(p + 4, 4);
-    } else if (m.type == 0x0008) {
-      const int ver = p[0];
-      if (ver >= 3) {
-        layout = p[1];
+    const std::vector<uint8_t> &v = m.data;
+    uint64_t x0, x1, x2;
+    if (m.type == 0x0001) {  // dataspace
+      if (!field(v, 0, 1, &x0) || !field(v, 1, 1, &x1)) return fail("bad dataspace");
+      const size_t o = x0 == 1 ? 8 : 4;
+      d.clear();
+      for (uint64_t k = 0; k < x1; ++k) {
+        uint64_t e;
+        if (!field(v, o + 8 * k, sl, &e)) return fail("bad dataspace");
+        d.push_back(e);
+      }
+    } else if (m.type == 0x0003) {  // datatype
+      if (!field(v, 0, 1, &x0) || !field(v, 1, 1, &x1) || !field(v, 4, 4, &x2)) return fail("bad datatype");
+      dclass = (int)(x0 & 0x0f);
+      big_endian = (x1 & 1) != 0;
+      dsize = (int)std::min<uint64_t>(x2, 1u << 20);
+    } else if (m.type == 0x0008) {  // data layout
+      if (!field(v, 0, 1, &x0)) return fail("bad layout");
+      if (x0 >= 3) {
+        if (!field(v, 1, 1, &x1)) return fail("bad layout");
+        layout = (int)x1;
         if (layout == 1) {
-          addr = rd(p + 2, so);
-          size = rd(p + 2 + so, sl);
+          if (!field(v, 2, so, &addr) || !field(v, 2 + so, sl, &size)) return fail("bad layout");
         } else if (layout == 0) {
-          const size_t n = rd(p + 2, 2);
-          compact.assign(p + 4, p + 4 + n);
+          if (!field(v, 2, 2, &x2) || x2 > v.size() - 4) return fail("bad layout");
+          compact.assign(v.begin() + 4, v.begin() + 4 + (size_t)x2);
         }
       } else {  // versions 1 and 2
-        const int rank = p[1];
-        layout = p[2];
+        if (!field(v, 1, 1, &x1) || !field(v, 2, 1, &x2)) return fail("bad layout");
+        const uint64_t rank = x1;
+        layout = (int)x2;
         size_t q = 8;
         if (layout != 0) {
-          addr = rd(p + q, so);
+          if (!field(v, q, so, &addr)) return fail("bad layout");
           q += so;
         }
-        uint64_t elems = 1;
-        for (int k = 0; k < rank; ++k) elems *= rd(p + q + 4 * k, 4);
-        size = elems;
         q += 4 * rank;
         if (layout == 0) {
-          const size_t n = rd(p + q, 4);
-          compact.assign(p + q + 4, p + q + 4 + n);
+          uint64_t cn;
+          if (!field(v, q, 4, &cn) || cn > v.size() - q - 4) return fail("bad layout");
+          compact.assign(v.begin() + q + 4, v.begin() + q + 4 + (size_t)cn);
         }
       }
     }
   }
   if (dclass != 1 || (dsize != 8 && dsize != 4) || big_endian) return fail("not a little-endian float dataset");
   uint64_t n = 1;
-  for (uint64_t x : d) n *= x;
+  for (uint64_t x : d) {
+    if (x != 0 && n > impl_->file_size / x) return fail("dataset larger than the file");
+    n *= x;
+  }
   std::vector<uint8_t> raw;
   if (layout == 1) {
     if (addr == UNDEF) {
+      if (n > (1ull << 40) / (uint64_t)dsize) return fail("dataset too large");
       raw.assign(n * dsize, 0);
     } else {
+      if (n > impl_->file_size / (uint64_t)dsize) return fail("dataset larger than the file");
       raw = impl_->read(addr, n * dsize);
       if (raw.size() != n * dsize) return fail("short read");
     }
   } else if (layout == 0) {
     raw = compact;
-    if (raw.size() < n * dsize) return fail("short compact data");
+    if (n > raw.size() / (uint64_t)dsize) return fail("short compact data");
   } else {
     return fail("chunked datasets are not read here");
   }
@@ -949,7 +1034,7 @@ bool File::attr_double(const std::string &object, const std::string &name, doubl
     float f;
     std::memcpy(&f, a.data.data(), 4);
     *v = f;
-  } else if (a.dclass == 0) {
+  } else if (a.dclass == 0 && a.dsize >= 1 && a.dsize <= 8) {
     long long i = (long long)rd(a.data.data(), a.dsize);
     if (a.is_signed && a.dsize < 8 && (i >> (8 * a.dsize - 1)) & 1) i -= 1LL << (8 * a.dsize);
     *v = (double)i;
@@ -963,7 +1048,8 @@ bool File::attr_double(const std::string &object, const std::string &name, doubl
 bool File::attr_int(const std::string &object, const std::string &name, long long *v, std::string *err) {
   uint64_t oh;
   Impl::Attr a;
-  if (!impl_ || !impl_->resolve(object, &oh) || !impl_->attribute(oh, name, &a) || a.nelem < 1 || a.dclass != 0) {
+  if (!impl_ || !impl_->resolve(object, &oh) || !impl_->attribute(oh, name, &a) || a.nelem < 1 || a.dclass != 0 ||
+      a.dsize < 1 || a.dsize > 8) {
     if (err) *err = "no integer attribute " + name + " on " + object;
     return false;
   }

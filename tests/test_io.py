@@ -264,3 +264,82 @@ def test_damaged_snapshot_files_are_reported_not_read(L, tmp_path):
         assert rc != 0 and err, name
     rc, q2, t, it, err = read(L, str(good) + ":/ite_0000", nx, ny)
     assert rc == 0 and np.array_equal(q2, q), err
+
+
+FUZZ_SCRIPT = r"""
+import sys, ctypes as C
+import numpy as np
+sys.path[:0] = [{repo!r}, {tests!r}]
+from test_io import io_lib, read
+L = io_lib()
+good, path, nx, ny = {good!r}, {path!r}, {nx}, {ny}
+data = open(good, "rb").read()
+rng = np.random.default_rng(23)
+cases = [data[:cut] for cut in range(0, len(data), max(1, len(data) // 300))]
+for k in range(800):  # a few random bytes anywhere
+    b = bytearray(data)
+    for i in rng.integers(0, len(b), int(rng.integers(1, 9))):
+        b[i] = int(rng.integers(0, 256))
+    cases.append(bytes(b))
+for k in range(400):  # an aligned 8-byte field set to an extreme or self-referring value
+    b = bytearray(data)
+    off = int(rng.integers(0, len(b) - 8)) & ~7
+    vals = [2**63, 2**64 - 1, 2**32, 2**16 - 1, len(data), off, off - 16 if off >= 16 else 0, 0]
+    v = vals[int(rng.integers(0, len(vals)))]
+    b[off:off + 8] = v.to_bytes(8, "little")
+    cases.append(bytes(b))
+for k in range(400):  # a 2-byte field (message sizes, counts) set to an extreme value
+    b = bytearray(data)
+    off = int(rng.integers(0, len(b) - 2)) & ~1
+    vals = [0, 1, 0xFFFF, 0x8000, 8, 16]
+    b[off:off + 2] = vals[int(rng.integers(0, len(vals)))].to_bytes(2, "little")
+    cases.append(bytes(b))
+for v in (0, 1, 3, 5, 16, 255):  # superblock offset / length sizes
+    for pos in (13, 14):
+        b = bytearray(data)
+        b[pos] = v
+        cases.append(bytes(b))
+out = (C.c_double * (4 * nx * ny))()
+n = C.c_int64()
+import os
+import fv2d_gb300 as fv
+prm = fv.default_params(Nx=nx, Ny=ny)
+q = np.ones((ny, nx, 4))
+qp = q.ctypes.data_as(C.POINTER(C.c_double))
+err = C.create_string_buffer(256)
+xmf = open(good[:-3] + ".xmf", "rb").read()
+read_ok = append_ok = 0
+for k, blob in enumerate(cases):
+    open(path, "wb").write(blob)
+    rc = read(L, path + ":/ite_0000", nx, ny)[0]
+    read_ok += rc == 0
+    for ds in (b"/ite_0000/rho", b"/x", b"/ite_0000"):
+        L.fv2d_h5_read_doubles(path.encode(), ds, out, 4 * nx * ny, C.byref(n))
+    if k % 4 == 0:  # appending a snapshot parses the existing root group
+        open(path[:-3] + ".xmf", "wb").write(xmf)
+        rc = L.fv2d_snapshot_write(os.path.dirname(path).encode(), b"fuzz", 0, 0, C.byref(prm), b"blast", 1, 0.5,
+                                   qp, err, 256)
+        append_ok += rc == 0
+print("done", len(cases), read_ok, append_ok, flush=True)
+"""
+
+
+def test_snapshot_reader_survives_malformed_files(L, tmp_path):
+    """Some 2000 malformed variants of a snapshot (truncations; random bytes;
+    offsets, lengths and counts set to extreme or self-referring values;
+    unsupported offset sizes) are read -- and a quarter of them appended to --
+    in a child process: every call returns, with an error or a result, and
+    the process neither crashes nor loops (the reader bounds every read by
+    the file and every walk)."""
+    import subprocess
+    import sys
+    nx, ny = 12, 7
+    p = fv.default_params(Nx=nx, Ny=ny)
+    q = np.random.default_rng(5).uniform(0.1, 2.0, (ny, nx, 4))
+    write(L, tmp_path, "run", 0, 1, p, "blast", 0, 0.0, q)
+    here = os.path.dirname(os.path.abspath(__file__))
+    script = FUZZ_SCRIPT.format(repo=os.path.dirname(here), tests=here, good=str(tmp_path / "run.h5"),
+                                path=str(tmp_path / "fuzz.h5"), nx=nx, ny=ny)
+    r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.returncode, r.stdout[-500:], r.stderr[-2000:])
+    assert r.stdout.startswith("done"), r.stdout
