@@ -217,6 +217,34 @@ def test_full_size_sedov_matches_oracle(gpu_lib):
     assert bits_equal(s2.get_cons(), u1)
 
 
+@pytest.mark.slow
+def test_sedov_benchmark_run_matches_oracle_after_1000_steps(gpu_lib):
+    """The benchmark run itself -- Sedov 2048^2, PLM + HLLC, CFL 0.8,
+    reflecting walls, 1000 iterations from the initial condition through
+    the device-driven loop -- bitwise against the oracle (OpenMP over the
+    host cores, ~30 s on 16 cores): every dt and the final fields."""
+    p = reference_params(Nx=2048, Ny=2048, gamma0=1.4, reconstruction=2, riemann_solver=1, CFL=0.8,
+                         boundary_x=1, boundary_y=1)
+    o, s = Oracle(p), gpu_sim(p)
+    o.init_problem("sedov")
+    s.init_problem("sedov")
+    dts = []
+    for _ in range(1000):
+        d = o.compute_dt()
+        dts.append(d[0])
+        o.update(d[0])
+    t, n, _ = s.advance(1000, 1e30)
+    assert n == 1000
+    log = s.step_log(1000)
+    assert len(log) == 1000 and bits_equal(log[:, 1], np.array(dts))
+    t_ref = 0.0
+    for d in dts:  # t += dt in binary64, in order (main.cpp:83)
+        t_ref += d
+    assert t == t_ref
+    assert bits_equal(s.get_prim(), o.get_prim())
+    assert o.counters() == s.counters()
+
+
 FULL_SIZE = {
     # KH 4096^2, CFL 0.7, periodic: mass, both momenta and energy are conserved
     "kh_4096": ("kh_step", dict(Nx=4096, Ny=4096, gamma0=1.4, reconstruction=2, riemann_solver=1, CFL=0.7,
