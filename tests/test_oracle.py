@@ -113,6 +113,37 @@ def test_smallest_grids_against_reference_headers(shape):
         assert bits_equal(o.get_cons(), r.get_cons()), c
 
 
+LONG_RUNS = [
+    dict(riemann_solver=1, reconstruction=2, boundary_x=1, boundary_y=1),
+    dict(riemann_solver=0, reconstruction=2, boundary_x=2, boundary_y=0, time_stepping=1),
+    dict(riemann_solver=2, reconstruction=2, boundary_x=2, boundary_y=1, gravity_mode=1, gy=-0.5),
+    dict(riemann_solver=0, reconstruction=2, boundary_x=2, boundary_y=1, gravity_mode=1, gy=-0.1, time_stepping=1,
+         thermal_conductivity_active=1, kappa=1e-3, viscosity_active=1, mu=1e-3),
+    dict(riemann_solver=1, reconstruction=0, boundary_x=0, boundary_y=2, well_balanced_flux_at_y_bc=1, gravity_mode=1,
+         gy=-0.5),
+]
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference cross-check build (oracle/_ref) not present")
+@pytest.mark.parametrize("k", range(len(LONG_RUNS)))
+def test_long_runs_against_reference_headers(k):
+    """30 iterations on a 64 x 48 grid from random states: every dt and the
+    final primitive and conservative fields."""
+    q0 = random_prim(48, 64, 40 + k)
+    p = reference_params(Nx=64, Ny=48, gamma0=1.4, CFL=0.6, **LONG_RUNS[k])
+    o, r = Oracle(p), RefSim(p)
+    o.set_prim(q0)
+    r.set_prim(q0)
+    for _ in range(30):
+        d = o.compute_dt()
+        dr = r.compute_dt()
+        assert bits_equal(d[0], dr)
+        o.update(d[0])
+        r.update(dr)
+    assert bits_equal(o.get_prim(), r.get_prim())
+    assert bits_equal(o.get_cons(), r.get_cons())
+
+
 @pytest.mark.skipif(not ref_available(), reason="reference cross-check build (oracle/_ref) not present")
 def test_reference_reads_floats():
     """The reference's ini reader returns float-rounded reals (GetFloat)."""
