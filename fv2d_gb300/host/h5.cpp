@@ -555,7 +555,7 @@ std::string xdmf_grid(const std::string &name, double t, const std::string &grou
 }  // namespace
 
 bool write_xdmf(const std::string &xmf_path, const std::string &h5name, const RootInfo &root, bool truncate,
-                const std::string &grid_name, double t, const std::string &group, std::string *err) {
+                bool unique, const std::string &grid_name, double t, const std::string &group, std::string *err) {
   std::string text;
   if (!truncate) {
     std::ifstream in(xmf_path, std::ios::binary);
@@ -564,10 +564,15 @@ bool write_xdmf(const std::string &xmf_path, const std::string &h5name, const Ro
       return false;
     }
     text.assign(std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>());
-    const size_t fl = std::strlen(XDMF_FOOTER);
-    if (text.size() >= fl) text.resize(text.size() - fl);
   } else {
     text = xdmf_header(h5name, root);
+    if (unique) text += XDMF_FOOTER;  // the reference writes the empty series first
+  }
+  if (unique || !truncate) {
+    // rewind over the footer: sizeof includes its terminating zero, so one
+    // more character goes (fseek(-sizeof(str_xdmf_footer), SEEK_END))
+    const size_t back = std::strlen(XDMF_FOOTER) + (unique ? 1 : 0);
+    text.resize(text.size() >= back ? text.size() - back : 0);
   }
   text += xdmf_grid(grid_name, t, group);
   text += XDMF_FOOTER;

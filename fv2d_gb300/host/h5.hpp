@@ -53,8 +53,11 @@ bool read_snapshot(const std::string &path, const std::string &group, int nx, in
 
 // XDMF sidecar (IOManager.h:22-73, 181-188, 238-240, 274-280): a new file
 // (truncate) or the previous text with one more grid before the footer.
+// unique: the one-file-per-run layout, where the reference rewinds
+// sizeof(footer) bytes -- the footer and the character before it -- before
+// each grid (IOManager.h:238-240, 274); the file is byte-identical to its.
 bool write_xdmf(const std::string &xmf_path, const std::string &h5name, const RootInfo &root, bool truncate,
-                const std::string &grid_name, double t, const std::string &group, std::string *err);
+                bool unique, const std::string &grid_name, double t, const std::string &group, std::string *err);
 
 // General access used by tests and tools.
 class File {

@@ -117,7 +117,7 @@ int fv2d_snapshot_write(const char *dir, const char *name, int multiple_outputs,
       std::snprintf(stem, sizeof stem, "%s_%04d", name, iteration);
       const std::string h5name = std::string(stem) + ".h5";
       if (!h5::write_multiple(base + h5name, r, iteration, t, q, &e) ||
-          !h5::write_xdmf(base + stem + ".xmf", h5name, r, true, stem, t, "", &e)) {
+          !h5::write_xdmf(base + stem + ".xmf", h5name, r, true, false, stem, t, "", &e)) {
         set_err(err, errlen, e);
         return FV2D_ERR_INVALID;
       }
@@ -127,7 +127,8 @@ int fv2d_snapshot_write(const char *dir, const char *name, int multiple_outputs,
     std::snprintf(gname, sizeof gname, "ite_%04d", iteration);
     const std::string h5name = std::string(name) + ".h5";
     if (!h5::write_unique(base + h5name, truncate != 0, r, iteration, t, q, &e) ||
-        !h5::write_xdmf(base + name + ".xmf", h5name, r, truncate != 0, gname, t, std::string(gname) + "/", &e)) {
+        !h5::write_xdmf(base + name + ".xmf", h5name, r, truncate != 0, true, gname, t, std::string(gname) + "/",
+                        &e)) {
       set_err(err, errlen, e);
       return FV2D_ERR_INVALID;
     }

@@ -343,3 +343,51 @@ def test_snapshot_reader_survives_malformed_files(L, tmp_path):
     r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, (r.returncode, r.stdout[-500:], r.stderr[-2000:])
     assert r.stdout.startswith("done"), r.stdout
+
+
+def _reference_xdmf_strings():
+    """The XDMF format strings of the reference's IOManager.h (raw-string literals)."""
+    import re
+    path = os.path.join(REF_DIR, "IOManager.h")
+    if not os.path.exists(path):
+        return None
+    text = open(path).read()
+    out = {}
+    for m in re.finditer(r'char (str_xdmf_\w+)\[\] =\s*R"xml\((.*?)\)xml";', text, flags=re.S):
+        out[m.group(1)] = m.group(2)
+    return out
+
+
+@pytest.mark.skipif(_reference_xdmf_strings() is None, reason="reference checkout not present")
+def test_xdmf_sidecars_are_byte_identical_to_the_references(L, tmp_path):
+    """The XDMF files that saveSolutionUnique / saveSolutionMultiple
+    (IOManager.h:107-279) write -- their printf formats applied in the same
+    order, including the unique mode's rewind of sizeof(footer) bytes before
+    each new grid -- against the library's files for the same snapshots."""
+    S = _reference_xdmf_strings()
+    c = lambda s: s.replace("%lf", "%f")  # noqa: E731  (C's %lf is %f)
+
+    def fields(group):
+        return (c(S["str_xdmf_scalar_field"]) % ("rho", group, "rho") +
+                c(S["str_xdmf_vector_field"]) % ("velocity", group, "u", group, "v") +
+                c(S["str_xdmf_scalar_field"]) % ("prs", group, "prs") + S["str_xdmf_ite_footer"])
+
+    d = tmp_path
+    nx, ny = 12, 7
+    p = fv.default_params(Nx=nx, Ny=ny)
+    q = np.ones((ny, nx, 4))
+    times = [0.0, 0.0125, 1.0 / 3.0]
+    footer = S["str_xdmf_footer"]
+    # unique file: header + footer, then per snapshot a rewind of sizeof(footer) = len + 1 bytes
+    ref = bytearray((c(S["str_xdmf_header"]) % ("run.h5", ny, nx, ny + 1, nx + 1) + footer).encode())
+    for k, t in enumerate(times):
+        write(L, d, "run", 0, 1 if k == 0 else 0, p, "blast", k, t, q)
+        name = "ite_%04d" % k
+        del ref[len(ref) - (len(footer) + 1):]
+        ref += (c(S["str_xdmf_ite_header"]) % (name, t) + fields(name + "/") + footer).encode()
+    assert (d / "run.xmf").read_bytes() == bytes(ref)
+    # one file per snapshot
+    write(L, d, "snap", 1, 1, p, "sod_x", 7, 0.5, q)
+    ref = (c(S["str_xdmf_header"]) % ("snap_0007.h5", ny, nx, ny + 1, nx + 1) +
+           c(S["str_xdmf_ite_header"]) % ("snap_0007", 0.5) + fields("") + footer)
+    assert (d / "snap_0007.xmf").read_bytes() == ref.encode()
