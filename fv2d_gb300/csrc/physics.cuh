@@ -62,6 +62,7 @@ __host__ __device__ __forceinline__ uint64_t fv_recip(double b) {
 #ifdef __CUDA_ARCH__
   return softfp::recip_of(b);
 #else
+  (void)b;
   return 0ull;
 #endif
 }
@@ -69,6 +70,7 @@ __host__ __device__ __forceinline__ double fv_div_by(double a, double b, uint64_
 #ifdef __CUDA_ARCH__
   return softfp::div_by(a, b, r);
 #else
+  (void)r;
   return a / b;
 #endif
 }

@@ -176,9 +176,9 @@ int main(int argc, char **argv) {
     resumed_after_save = false;
     t = td;
     if (status == FV2D_RUN_SAVE) {  // main.cpp:64-77: dt line, save, then the update
-      double dt, ih, itc, iv;
-      fv2d_compute_dt(r.ctx, &dt, &ih, &itc, &iv);
-      if (next_log == 0) print_dt(r, t, ih, itc, iv);
+      double dt, ih, itc_s, iv_s;
+      fv2d_compute_dt(r.ctx, &dt, &ih, &itc_s, &iv_s);
+      if (next_log == 0) print_dt(r, t, ih, itc_s, iv_s);
       next_log = next_log == 0 ? r.p.log_frequency : next_log - 1;
       std::cout << " - Saving at time " << t << std::endl;
       if (!save(r, ite++, t)) return 1;
