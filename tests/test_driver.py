@@ -5,7 +5,6 @@ snapshot is compared bit for bit with the oracle run through the same loop
 import os
 import subprocess
 
-import numpy as np
 import pytest
 
 from fv2d_testlib import Oracle, bits_equal, reference_params
