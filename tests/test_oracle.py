@@ -179,7 +179,8 @@ def test_negative_reset_counters():
     assert (o.get_prim()[..., 0] > 0).all()
 
 
-def test_sod_converges_to_the_exact_riemann_solution():
+@pytest.mark.parametrize("recon", [2, 3])  # PLM; MUSCL-Hancock (the benchmark's CPU set-up, no reference counterpart)
+def test_sod_converges_to_the_exact_riemann_solution(recon):
     """Physics check of the scheme the oracle restates (and the GPU path
     reproduces bit for bit): the Sod problem of the benchmark set-up against
     the exact Riemann solution (tests/exact_riemann.py), in L1 for rho, u
@@ -189,7 +190,7 @@ def test_sod_converges_to_the_exact_riemann_solution():
     errs = {}
     for nx in (128, 512):
         p = reference_params(Nx=nx, Ny=8, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0 / 64, gamma0=1.4,
-                             reconstruction=2, riemann_solver=1, CFL=0.8, boundary_x=0, boundary_y=2, tend=0.2)
+                             reconstruction=recon, riemann_solver=1, CFL=0.8, boundary_x=0, boundary_y=2, tend=0.2)
         o = Oracle(p)
         o.init_problem("sod_x")
         t, _ = o.run(p.tend, 100000)
