@@ -101,6 +101,28 @@ def test_odd_sizes_match_oracle(gpu_lib, shape):
         s.close()
 
 
+def test_sod_benchmark_with_muscl_hancock_matches_oracle(gpu_lib):
+    """The CPU-runnable benchmark set-up as specified -- Sod 512x8, PLM slopes
+    with the MUSCL-Hancock half-step, HLLC, CFL 0.8, outflow in x, periodic
+    in y, to t = 0.2 -- through the device loop, bitwise against the oracle
+    (every dt, t, the fields)."""
+    p = reference_params(Nx=512, Ny=8, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0 / 64, gamma0=1.4, reconstruction=3,
+                         riemann_solver=1, CFL=0.8, boundary_x=0, boundary_y=2, tend=0.2)
+    o, s = Oracle(p), gpu_sim(p)
+    o.init_problem("sod_x")
+    s.init_problem("sod_x")
+    dts, t_ref = [], 0.0
+    while t_ref + p.epsilon < p.tend:
+        d = o.compute_dt()
+        dts.append(d[0])
+        o.update(d[0])
+        t_ref += d[0]
+    t, n, _ = s.advance(100000, p.tend)
+    assert n == len(dts) and t == t_ref
+    assert bits_equal(s.step_log(4096)[:, 1], np.array(dts))
+    assert bits_equal(s.get_prim(), o.get_prim())
+
+
 def test_muscl_hancock_extension_matches_oracle(gpu_lib):
     q0 = random_prim(19, 37, 5, smooth=True)
     for rs in (0, 1, 2):
