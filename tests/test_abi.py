@@ -116,3 +116,16 @@ def test_server_rejects_bad_configs_without_gpu(libs):
     cfg = ServerConfig(C.sizeof(ServerConfig) - 8, **good)
     h = C.c_void_p()
     assert lib.fv2d_server_create(C.byref(cfg), C.byref(h)) == _abi.ERR_INVALID
+
+
+def test_no_cpu_fallback_without_a_gpu(libs):
+    """Without a usable GPU the library refuses loudly (FV2D_ERR_CUDA and the
+    CUDA message); nothing falls back to a CPU path."""
+    from fv2d_gb300 import Fv2dError, Simulation, default_params
+    try:
+        s = Simulation(default_params(Nx=32, Ny=32))
+    except Fv2dError as e:
+        assert e.code == _abi.ERR_CUDA and "CUDA" in str(e)
+        return
+    s.close()
+    pytest.skip("a GPU is present")
