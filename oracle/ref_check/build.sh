@@ -14,3 +14,9 @@ ${CXX:-g++} -std=c++20 -O2 -ffp-contract=off -fPIC -shared -w \
   -I"$HERE/include" -I"$REF_DIR" \
   -o "$OUT/libfv2d_ref.so" "$HERE/ref_harness.cpp"
 echo "built $OUT/libfv2d_ref.so"
+# the same sources with OpenMP over rows (a release-style build of the
+# reference's step code for timing it on the host cores)
+${CXX:-g++} -std=c++20 -O3 -fopenmp -ffp-contract=off -fPIC -shared -w \
+  -I"$HERE/include" -I"$REF_DIR" \
+  -o "$OUT/libfv2d_ref_omp.so" "$HERE/ref_harness.cpp"
+echo "built $OUT/libfv2d_ref_omp.so"

@@ -4,7 +4,9 @@
 // Update.h, ThermalConduction.h, Viscosity.h, ComputeDt.h, Init.h).  It lets
 // those headers compile unchanged with g++ so that their arithmetic can be run
 // on the CPU and compared with the oracle.  Nothing here is Kokkos code; it is
-// written for this repository and implements only serial semantics:
+// written for this repository and implements only these semantics (serial,
+// or with OpenMP over rows when compiled with -fopenmp, to time the reference's
+// own step code on the host cores):
 //   - View<double***>: zero-initialised, shallow-copy (shared) storage,
 //     operator()(i0, i1, i2) row-major;
 //   - MDRangePolicy<Rank<2>>: [b0, e0) x [b1, e1), functor called as f(i0, i1);
@@ -50,19 +52,42 @@ struct Array {
 template <class T>
 class View;
 
+namespace detail {
+// Like Kokkos, views copied while a parallel dispatch runs do not take part in
+// reference counting (the kernel's captured views keep the data alive): the
+// copies the kernels make per cell then cost a pointer copy, not an atomic.
+inline int &tracking_off() {
+  static int off = 0;
+  return off;
+}
+}  // namespace detail
+
 template <class T>
 class View<T ***> {
  public:
   View() = default;
   View(const std::string &, std::size_t n0, std::size_t n1, std::size_t n2)
-      : d_(std::make_shared<std::vector<T>>(n0 * n1 * n2, T(0))), n0_(n0), n1_(n1), n2_(n2) {}
-  T &operator()(std::size_t a, std::size_t b, std::size_t c) const { return (*d_)[(a * n1_ + b) * n2_ + c]; }
+      : owner_(std::make_shared<std::vector<T>>(n0 * n1 * n2, T(0))), p_(owner_->data()), n0_(n0), n1_(n1),
+        n2_(n2) {}
+  View(const View &o) : p_(o.p_), n0_(o.n0_), n1_(o.n1_), n2_(o.n2_) {
+    if (!detail::tracking_off()) owner_ = o.owner_;
+  }
+  View &operator=(const View &o) {
+    if (!detail::tracking_off()) owner_ = o.owner_;
+    p_ = o.p_;
+    n0_ = o.n0_;
+    n1_ = o.n1_;
+    n2_ = o.n2_;
+    return *this;
+  }
+  T &operator()(std::size_t a, std::size_t b, std::size_t c) const { return p_[(a * n1_ + b) * n2_ + c]; }
   std::size_t extent(int k) const { return k == 0 ? n0_ : (k == 1 ? n1_ : n2_); }
-  T *data() const { return d_ ? d_->data() : nullptr; }
+  T *data() const { return p_; }
   std::size_t size() const { return n0_ * n1_ * n2_; }
 
  private:
-  std::shared_ptr<std::vector<T>> d_;
+  std::shared_ptr<std::vector<T>> owner_;
+  T *p_ = nullptr;
   std::size_t n0_ = 0, n1_ = 0, n2_ = 0;
 };
 
@@ -89,8 +114,13 @@ struct MDRangePolicy<Rank<2>> {
 
 template <class F>
 void parallel_for(const std::string &, const MDRangePolicy<Rank<2>> &p, const F &f) {
+  detail::tracking_off() = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
   for (long i1 = p.b_[1]; i1 < p.e_[1]; ++i1)
     for (long i0 = p.b_[0]; i0 < p.e_[0]; ++i0) f((int)i0, (int)i1);
+  detail::tracking_off() = 0;
 }
 
 template <class T>
@@ -115,6 +145,8 @@ struct slot {  // plain lvalue target: sum reduction
   value_type local;
   value_type &target;
   explicit slot(X &t) : local(0), target(t) {}
+  static value_type identity() { return value_type(0); }
+  void join(const value_type &v) { local += v; }
   void finish() { target = local; }
 };
 template <class T>
@@ -123,6 +155,8 @@ struct slot<Max<T>> {
   value_type local;
   T &target;
   explicit slot(Max<T> &m) : local(Max<T>::identity()), target(m.ref) {}
+  static value_type identity() { return Max<T>::identity(); }
+  void join(const value_type &v) { Max<T>::join(local, v); }
   void finish() { target = local; }
 };
 }  // namespace detail
@@ -135,8 +169,30 @@ void parallel_reduce(const std::string &, const MDRangePolicy<Rank<2>> &p, const
   SA sa(a);
   SB sb(b);
   SC sc(c);
+  detail::tracking_off() = 1;
+#ifdef _OPENMP
+  // per-thread partial results joined at the end; the reductions used are
+  // maxima and integer counts, which do not depend on the order
+#pragma omp parallel
+  {
+    typename SA::value_type la = SA::identity();
+    typename SB::value_type lb = SB::identity();
+    typename SC::value_type lc = SC::identity();
+#pragma omp for schedule(static)
+    for (long i1 = p.b_[1]; i1 < p.e_[1]; ++i1)
+      for (long i0 = p.b_[0]; i0 < p.e_[0]; ++i0) f((int)i0, (int)i1, la, lb, lc);
+#pragma omp critical
+    {
+      sa.join(la);
+      sb.join(lb);
+      sc.join(lc);
+    }
+  }
+#else
   for (long i1 = p.b_[1]; i1 < p.e_[1]; ++i1)
     for (long i0 = p.b_[0]; i0 < p.e_[0]; ++i0) f((int)i0, (int)i1, sa.local, sb.local, sc.local);
+#endif
+  detail::tracking_off() = 0;
   sa.finish();
   sb.finish();
   sc.finish();
