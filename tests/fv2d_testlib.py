@@ -149,28 +149,42 @@ class Oracle:
 _ref_lib = None
 
 
-def ref_available():
-    return os.path.exists(REF_SO)
+REF_OMP_SO = os.path.join(REPO, "oracle", "_ref", "libfv2d_ref_omp.so")
+_ref_libs = {}
 
 
-def ref_lib():
+def ref_available(path=None):
+    return os.path.exists(path or REF_SO)
+
+
+def ref_lib(path=None):
+    """The reference-header library: the serial parity build, or another
+    build of the same sources (e.g. REF_OMP_SO, OpenMP over rows)."""
     global _ref_lib
+    path = path or REF_SO
+    if path != REF_SO:
+        if path not in _ref_libs:
+            _ref_libs[path] = _bind_ref(C.CDLL(path))
+        return _ref_libs[path]
     if _ref_lib is None:
-        lib = C.CDLL(REF_SO)
-        lib.fv2d_ref_create.restype = C.c_void_p
-        lib.fv2d_ref_create.argtypes = [C.c_char_p]
-        lib.fv2d_ref_destroy.argtypes = [C.c_void_p]
-        lib.fv2d_ref_dims.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
-        lib.fv2d_ref_param.argtypes = [C.c_void_p, C.c_char_p, _dbl_p]
-        lib.fv2d_ref_init.argtypes = [C.c_void_p]
-        lib.fv2d_ref_set_prim.argtypes = [C.c_void_p, _dbl_p]
-        lib.fv2d_ref_get_prim.argtypes = [C.c_void_p, _dbl_p]
-        lib.fv2d_ref_get_cons.argtypes = [C.c_void_p, _dbl_p]
-        lib.fv2d_ref_compute_dt.restype = C.c_double
-        lib.fv2d_ref_compute_dt.argtypes = [C.c_void_p, C.c_int]
-        lib.fv2d_ref_update.argtypes = [C.c_void_p, C.c_double]
-        _ref_lib = lib
+        _ref_lib = _bind_ref(C.CDLL(REF_SO))
     return _ref_lib
+
+
+def _bind_ref(lib):
+    lib.fv2d_ref_create.restype = C.c_void_p
+    lib.fv2d_ref_create.argtypes = [C.c_char_p]
+    lib.fv2d_ref_destroy.argtypes = [C.c_void_p]
+    lib.fv2d_ref_dims.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.fv2d_ref_param.argtypes = [C.c_void_p, C.c_char_p, _dbl_p]
+    lib.fv2d_ref_init.argtypes = [C.c_void_p]
+    lib.fv2d_ref_set_prim.argtypes = [C.c_void_p, _dbl_p]
+    lib.fv2d_ref_get_prim.argtypes = [C.c_void_p, _dbl_p]
+    lib.fv2d_ref_get_cons.argtypes = [C.c_void_p, _dbl_p]
+    lib.fv2d_ref_compute_dt.restype = C.c_double
+    lib.fv2d_ref_compute_dt.argtypes = [C.c_void_p, C.c_int]
+    lib.fv2d_ref_update.argtypes = [C.c_void_p, C.c_double]
+    return lib
 
 
 _BC = {0: "absorbing", 1: "reflecting", 2: "periodic"}
@@ -273,8 +287,8 @@ perturbation={r(p.c91_pert)}
 class RefSim:
     """The reference's own headers driven through oracle/_ref (CPU, serial)."""
 
-    def __init__(self, params, problem="blast"):
-        self.lib = ref_lib()
+    def __init__(self, params, problem="blast", lib_path=None):
+        self.lib = ref_lib(lib_path)
         fd, self.path = tempfile.mkstemp(suffix=".ini")
         with os.fdopen(fd, "w") as f:
             f.write(params_to_ini(params, problem))

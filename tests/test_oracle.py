@@ -5,7 +5,7 @@ headers directly."""
 import numpy as np
 import pytest
 
-from fv2d_testlib import (Oracle, RefSim, bits_equal, random_prim, ref_available, reference_params)
+from fv2d_testlib import (REF_OMP_SO, Oracle, RefSim, bits_equal, random_prim, ref_available, reference_params)
 import golden.make_golden as G
 
 
@@ -229,3 +229,23 @@ def test_restart_is_not_bit_exact_against_continuing():
     qa, qb = a.get_prim(), b.get_prim()
     assert not bits_equal(qa, qb)
     assert np.max(np.abs(qa - qb) / np.abs(qa).max(axis=(0, 1))) < 1e-9
+
+
+@pytest.mark.skipif(not ref_available(REF_OMP_SO), reason="OpenMP build of the reference headers not present")
+def test_openmp_build_of_the_reference_headers_matches_the_oracle():
+    """The build used to time the reference's own step code on the host
+    cores (OpenMP over rows) gives the oracle's bits: its timing is a timing
+    of the same arithmetic."""
+    q0 = random_prim(64, 96, 7)
+    for c in LONG_RUNS[:3]:
+        p = reference_params(Nx=96, Ny=64, gamma0=1.4, CFL=0.6, **c)
+        o, r = Oracle(p), RefSim(p, lib_path=REF_OMP_SO)
+        o.set_prim(q0)
+        r.set_prim(q0)
+        for _ in range(10):
+            d = o.compute_dt()
+            dr = r.compute_dt()
+            assert bits_equal(d[0], dr)
+            o.update(d[0])
+            r.update(dr)
+        assert bits_equal(o.get_prim(), r.get_prim())
