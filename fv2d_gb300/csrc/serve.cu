@@ -18,6 +18,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -300,6 +301,12 @@ struct fv2d_server {
   cudaStream_t bstream[kBuckets] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kBuckets] = {};
   double sched_cells = 0;  // cells advanced per step by the current work lists
+  // failure state: `fault` is written by the worker alone; `broken`,
+  // `fail_code` and `err` are set once, under mu, when the worker stops
+  std::string fault;
+  std::atomic<bool> inject{false};
+  bool broken = false;
+  int fail_code = FV2D_OK;
   std::string err;
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
@@ -337,6 +344,15 @@ const char *check_request(const fv2d_request &r) {
     return "constant conductivity without boundary modes only";
   if (r.max_steps < 0) return "max_steps < 0";
   return nullptr;
+}
+
+// Synchronises the worker's stream.  A failure is recorded in s->fault: the
+// context is then unusable, and the worker stops after this iteration.
+bool sync_stream(fv2d_server *s) {
+  const cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (e == cudaSuccess) return true;
+  if (s->fault.empty()) s->fault = std::string("CUDA: ") + cudaGetErrorString(e);
+  return false;
 }
 
 size_t state_bytes(int N, int *pitch, long long *plane) {
@@ -496,7 +512,7 @@ void read_initial_cons(fv2d_server *s, const std::vector<int> &fresh) {
   for (int slot : fresh)
     cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
                     sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
-  cudaStreamSynchronize(s->stream);
+  if (!sync_stream(s)) return;
   for (int slot : fresh) {
     Slot &sl = s->slots[slot];
     const fv2d_params &p = sl.req.params;
@@ -638,12 +654,16 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
       cudaGetLastError();
   }
   // page-locked staging when it could be had, else pageable memory (the same
-  // copies, without overlap)
+  // copies, without overlap); with neither, the requests complete with
+  // FV2D_ERR_NOMEM and no final state
   std::vector<float> pageable;
   float *stage = s->h_stage;
   if (!stage) {
-    pageable.resize(need);
-    stage = pageable.data();
+    try {
+      pageable.resize(need);
+      stage = pageable.data();
+    } catch (const std::bad_alloc &) {
+    }
   }
   for (size_t k = 0; k < done.size(); ++k) {
     const int slot = done[k];
@@ -652,7 +672,7 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
     cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
     cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
                     sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
-    for (int f = 0; f < 4; ++f)
+    for (int f = 0; f < 4 && stage; ++f)
       cudaMemcpy2DAsync(stage + off[k] + (size_t)f * N * N, sizeof(float) * N,
                         d.U[d.cur] + f * d.plane + 2 * d.pitch + 2, sizeof(float) * d.pitch, sizeof(float) * N, N,
                         cudaMemcpyDeviceToHost, s->stream);
@@ -661,7 +681,7 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
     cudaMemcpyAsync(&s->d_sims[slot].status, &s->h_up[slot].status, sizeof(int), cudaMemcpyHostToDevice,
                     s->stream);
   }
-  cudaStreamSynchronize(s->stream);
+  if (!sync_stream(s)) return;  // the slots stay resident; the worker fails them
   const double t_done = s->now();
   for (size_t k = 0; k < done.size(); ++k) {
     const int slot = done[k];
@@ -688,7 +708,15 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
       r.cons0[f] = sl.cons0[f];
       r.cons1[f] = c1[f] * area;
     }
-    fin.U.assign(stage + off[k], stage + off[k] + 4 * (size_t)N * N);
+    bool kept = false;
+    if (stage) {
+      try {
+        fin.U.assign(stage + off[k], stage + off[k] + 4 * (size_t)N * N);
+        kept = true;
+      } catch (const std::bad_alloc &) {
+      }
+    }
+    if (!kept && r.status == FV2D_OK) r.status = FV2D_ERR_NOMEM;
     fin.gamma = p.gamma0;
     r.done_s = t_done;
     s->arena.release(sl.mem, sl.bytes);
@@ -704,8 +732,11 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
       s->n_completed++;
     else
       s->n_failed++;
-    s->done_unpolled.push_back(r);
-    s->finished.emplace(r.id, std::move(fin));
+    try {
+      s->done_unpolled.push_back(r);
+      if (kept) s->finished.emplace(r.id, std::move(fin));
+    } catch (const std::bad_alloc &) {  // counted; its record or final state is lost
+    }
   }
   s->cv.notify_all();
 }
@@ -740,7 +771,7 @@ bool run_once(fv2d_server *s, int K_fixed) {
   for (int k = 0; k < s->max_sims; ++k)
     if (s->slots[k].used) hi = k + 1;
   cudaMemcpyAsync(s->h_down, s->d_sims, sizeof(SimDev) * hi, cudaMemcpyDeviceToHost, s->stream);
-  cudaStreamSynchronize(s->stream);
+  if (!sync_stream(s)) return true;
   float ms = 0;
   cudaEventElapsedTime(&ms, s->ev0, s->ev1);
   s->replays++;
@@ -764,44 +795,112 @@ bool run_once(fv2d_server *s, int K_fixed) {
   return true;
 }
 
+// The worker cannot go on: its stream failed (the CUDA context is then
+// unusable), or host memory ran out while it changed its tables.  Every
+// resident request, every queued one and the ones in `extra` (taken from the
+// queue and not yet admitted) complete with `code`; later submissions are
+// refused.  Device memory stays with the server until fv2d_server_destroy.
+void fail_all(fv2d_server *s, int code, const std::vector<Pending> &extra) noexcept {
+  const double t = s->now();
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->broken = true;
+  s->fail_code = code;
+  try {
+    s->err = s->fault.empty() ? std::string("service stopped") : s->fault;
+  } catch (const std::bad_alloc &) {
+  }
+  auto post = [&](int64_t id, double submit_s, double admit_s, int N, int steps) {
+    fv2d_result r;
+    std::memset(&r, 0, sizeof(r));
+    r.id = id;
+    r.status = code;
+    r.steps = steps;
+    r.submit_s = submit_s;
+    r.admit_s = admit_s;
+    r.done_s = t;
+    r.N = N;
+    r.bucket = bucket_of(N);
+    s->n_failed++;
+    try {
+      s->done_unpolled.push_back(r);
+    } catch (const std::bad_alloc &) {  // counted; its record is lost
+    }
+  };
+  for (Slot &sl : s->slots)
+    if (sl.used) {
+      post(sl.id, sl.submit_s, sl.admit_s, sl.req.params.Nx, sl.steps_seen);
+      sl.used = false;
+    }
+  for (const Pending &pd : s->queue) post(pd.id, pd.submit_s, -1.0, pd.req.params.Nx, 0);
+  for (const Pending &pd : extra) post(pd.id, pd.submit_s, -1.0, pd.req.params.Nx, 0);
+  s->queue.clear();
+  s->n_active = 0;
+  publish_locked(s);
+  s->cv.notify_all();
+}
+
 void worker_main(fv2d_server *s) {
   cudaSetDevice(s->device);
   while (!s->stop.load()) {
-    std::vector<Pending> take;
-    {
-      std::unique_lock<std::mutex> lock(s->mu);
-      bool active = false;
-      for (auto &sl : s->slots)
-        if (sl.used) {
-          active = true;
-          break;
-        }
-      if (!active && s->queue.empty())
-        s->cv.wait_for(lock, std::chrono::milliseconds(20));
-      take.assign(s->queue.begin(), s->queue.end());
-      s->queue.clear();
+    std::vector<Pending> take, keep;
+    size_t next = 0;  // entries of `take` before this one were admitted or moved to `keep`
+    try {
+      {
+        std::unique_lock<std::mutex> lock(s->mu);
+        bool active = false;
+        for (auto &sl : s->slots)
+          if (sl.used) {
+            active = true;
+            break;
+          }
+        if (!active && s->queue.empty())
+          s->cv.wait_for(lock, std::chrono::milliseconds(20));
+        take.assign(s->queue.begin(), s->queue.end());
+        s->queue.clear();
+      }
+      // admission: first in, first out; a request that does not fit waits and
+      // smaller ones behind it may pass
+      std::vector<int> fresh;
+      fresh.reserve(take.size());  // no allocation once a request is admitted
+      keep.reserve(take.size());
+      for (; next < take.size(); ++next) {
+        const int slot = admit(s, take[next]);
+        if (slot >= 0)
+          fresh.push_back(slot);
+        else
+          keep.push_back(take[next]);
+      }
+      if (!keep.empty()) {
+        std::lock_guard<std::mutex> lock(s->mu);
+        std::deque<Pending> q(keep.begin(), keep.end());
+        q.insert(q.end(), s->queue.begin(), s->queue.end());
+        s->queue.swap(q);
+      }
+      keep.clear();
+      take.clear();
+      next = 0;
+      read_initial_cons(s, fresh);
+      if (!fresh.empty()) {
+        std::lock_guard<std::mutex> lock(s->mu);
+        publish_locked(s);
+      }
+      if (s->fault.empty()) run_once(s, s->cfg.steps_per_replay);
+      if (s->fault.empty() && s->inject.exchange(false)) s->fault = "simulated failure (fv2d_server_inject_fault)";
+      if (!s->fault.empty()) {
+        fail_all(s, FV2D_ERR_CUDA, {});
+        return;
+      }
+    } catch (const std::exception &e) {
+      std::vector<Pending> extra;
+      try {
+        extra = keep;
+        extra.insert(extra.end(), take.begin() + next, take.end());
+        s->fault = std::string("host: ") + e.what();
+      } catch (const std::bad_alloc &) {
+      }
+      fail_all(s, FV2D_ERR_NOMEM, extra);
+      return;
     }
-    // admission: first in, first out; a request that does not fit waits and
-    // smaller ones behind it may pass
-    std::vector<Pending> keep;
-    std::vector<int> fresh;
-    for (auto &pd : take) {
-      const int slot = admit(s, pd);
-      if (slot >= 0)
-        fresh.push_back(slot);
-      else
-        keep.push_back(pd);
-    }
-    if (!keep.empty()) {
-      std::lock_guard<std::mutex> lock(s->mu);
-      for (auto it = keep.rbegin(); it != keep.rend(); ++it) s->queue.push_front(*it);
-    }
-    read_initial_cons(s, fresh);
-    if (!fresh.empty()) {
-      std::lock_guard<std::mutex> lock(s->mu);
-      publish_locked(s);
-    }
-    run_once(s, s->cfg.steps_per_replay);
   }
 }
 
@@ -983,6 +1082,7 @@ int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id) {
   long long plane;
   if ((double)state_bytes(req->params.Nx, &pitch, &plane) > s->cfg.budget_bytes) return FV2D_ERR_SIZE;
   std::lock_guard<std::mutex> lock(s->mu);
+  if (s->broken) return FV2D_ERR_STATE;
   Pending pd;
   pd.id = s->next_id++;
   pd.req = *req;
@@ -1005,10 +1105,11 @@ int fv2d_server_poll(fv2d_server *s, fv2d_result *out, int max, int *n) {
 }
 
 int fv2d_server_drain(fv2d_server *s, double timeout_s) {
-  if (!s) return FV2D_ERR_INVALID;
+  if (!s || !(timeout_s >= 0)) return FV2D_ERR_INVALID;
   const double end = s->now() + timeout_s;
   std::unique_lock<std::mutex> lock(s->mu);
   for (;;) {
+    if (s->broken) return s->fail_code;
     const bool idle = s->queue.empty() && (s->n_completed + s->n_failed) == s->n_submitted;
     if (idle) return FV2D_OK;
     if (s->now() > end) return FV2D_ERR_STATE;
@@ -1040,6 +1141,20 @@ int fv2d_server_release(fv2d_server *s, int64_t id) {
   if (!s) return FV2D_ERR_INVALID;
   std::lock_guard<std::mutex> lock(s->mu);
   return s->finished.erase(id) ? FV2D_OK : FV2D_ERR_STATE;
+}
+
+int fv2d_server_last_error(fv2d_server *s, char *buf, int len) {
+  if (!s || !buf || len <= 0) return FV2D_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  std::snprintf(buf, (size_t)len, "%s", s->err.c_str());
+  return FV2D_OK;
+}
+
+int fv2d_server_inject_fault(fv2d_server *s) {
+  if (!s) return FV2D_ERR_INVALID;
+  s->inject.store(true);
+  s->cv.notify_all();
+  return FV2D_OK;
 }
 
 int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out) {

@@ -6,7 +6,7 @@ import math
 import numpy as np
 
 from . import lib as _lib_loader
-from ._abi import Params, PROBLEMS, as_float32
+from ._abi import ERR_STATE, Params, PROBLEMS, as_float32
 
 
 class ServerConfig(C.Structure):
@@ -53,6 +53,8 @@ def _bind(L):
     L.fv2d_server_get_prim.argtypes = [vp, C.c_int64, C.POINTER(C.c_double)]
     L.fv2d_server_release.argtypes = [vp, C.c_int64]
     L.fv2d_server_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.fv2d_server_last_error.argtypes = [vp, C.c_char_p, C.c_int]
+    L.fv2d_server_inject_fault.argtypes = [vp]
     L.fv2d_server_config_name.argtypes = [C.c_int]
     L.fv2d_server_config_name.restype = C.c_char_p
     L._serve_bound = True
@@ -121,6 +123,8 @@ class Server:
         r = Request(C.sizeof(Request), pb, params, int(max_steps), 1 if lowmach else 0, float(tend))
         i = C.c_int64()
         rc = self.L.fv2d_server_submit(self.h, C.byref(r), C.byref(i))
+        if rc == ERR_STATE:
+            raise RuntimeError(f"the service has stopped: {self.last_error()}")
         if rc != 0:
             raise ValueError(f"request rejected ({rc})")
         self._n[i.value] = params.Nx
@@ -133,7 +137,19 @@ class Server:
         return [out[k] for k in range(n.value)]
 
     def drain(self, timeout_s=600.0):
+        """0 once nothing is queued or running; ERR_STATE on timeout; the
+        stopping code (ERR_CUDA, ERR_NOMEM) once the service has stopped."""
         return self.L.fv2d_server_drain(self.h, float(timeout_s))
+
+    def last_error(self):
+        """Why the service stopped ('' while it runs)."""
+        buf = C.create_string_buffer(512)
+        self.L.fv2d_server_last_error(self.h, buf, len(buf))
+        return buf.value.decode(errors="replace")
+
+    def inject_fault(self):
+        """Test hook: the worker stops as if a CUDA call had failed."""
+        self.L.fv2d_server_inject_fault(self.h)
 
     def get_prim(self, rid):
         N = self._n[rid]

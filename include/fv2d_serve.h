@@ -22,6 +22,19 @@
  *   - tile shape, threads per tile and halo staging are chosen per bucket by
  *     an autotuner at start-up (or fixed defaults).
  * A simulation's result does not depend on what else was in the batch.
+ *
+ * Failures:
+ *   - a request whose dt guard trips completes with FV2D_ERR_NUMERIC; the
+ *     others are not affected;
+ *   - a request whose final state cannot be copied to host memory completes
+ *     with FV2D_ERR_NOMEM and keeps no state;
+ *   - if a CUDA call of the worker fails (the CUDA context is then unusable),
+ *     or host memory runs out while the worker changes its tables, the
+ *     service stops: every resident and queued request completes with
+ *     FV2D_ERR_CUDA (resp. FV2D_ERR_NOMEM), fv2d_server_submit returns
+ *     FV2D_ERR_STATE, fv2d_server_drain returns that code at once and
+ *     fv2d_server_last_error says what failed.  Device memory is released by
+ *     fv2d_server_destroy.
  */
 #ifndef FV2D_SERVE_H
 #define FV2D_SERVE_H
@@ -92,7 +105,9 @@ int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id);
 /* Results completed since the last poll (at most max); *n receives the count. */
 int fv2d_server_poll(fv2d_server *s, fv2d_result *out, int max, int *n);
 
-/* Block until nothing is queued or running (or timeout_s elapses). */
+/* Block until nothing is queued or running: FV2D_OK; FV2D_ERR_STATE when
+ * timeout_s (>= 0, may be infinite) elapses first; the stopping code when the
+ * service has stopped (see Failures above). */
 int fv2d_server_drain(fv2d_server *s, double timeout_s);
 
 /* Final primitive state of a completed request (N x N x {rho,u,v,p}, binary64
@@ -101,6 +116,14 @@ int fv2d_server_get_prim(fv2d_server *s, int64_t id, double *q_host);
 int fv2d_server_release(fv2d_server *s, int64_t id);
 
 int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out);
+
+/* Why the service stopped ("" while it runs), copied into buf (len bytes at
+ * most, NUL-terminated).  Thread-safe. */
+int fv2d_server_last_error(fv2d_server *s, char *buf, int len);
+
+/* Test hook for the failure path above, with no GPU fault: the worker stops
+ * after its current replay as if a CUDA call had failed. */
+int fv2d_server_inject_fault(fv2d_server *s);
 
 /* Name of tile configuration `index` ("32x16/256/tma", ...); NULL if none. */
 const char *fv2d_server_config_name(int index);

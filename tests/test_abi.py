@@ -116,6 +116,11 @@ def test_server_rejects_bad_configs_without_gpu(libs):
     cfg = ServerConfig(C.sizeof(ServerConfig) - 8, **good)
     h = C.c_void_p()
     assert lib.fv2d_server_create(C.byref(cfg), C.byref(h)) == _abi.ERR_INVALID
+    # calls on no server
+    buf = C.create_string_buffer(16)
+    assert lib.fv2d_server_last_error(None, buf, 16) == _abi.ERR_INVALID
+    assert lib.fv2d_server_inject_fault(None) == _abi.ERR_INVALID
+    assert lib.fv2d_server_drain(None, 1.0) == _abi.ERR_INVALID
 
 
 def test_no_cpu_fallback_without_a_gpu(libs):

@@ -8,6 +8,9 @@
   FV2D_ERR_NUMERIC while the requests batched with it finish with the same
   results as alone; a request that can never fit the memory budget is refused
   at submission.
+* A failure of the served worker's CUDA stream, simulated on the host by the
+  library's test hook: every resident and queued request completes with
+  FV2D_ERR_CUDA, drain returns that code, and later submissions are refused.
 """
 import numpy as np
 import pytest
@@ -97,3 +100,32 @@ def test_served_refuses_a_request_larger_than_the_budget(gpu_lib):
     with Server(budget_bytes=1e6, autotune=False) as s:  # a 256^2 state pair needs 2.4 MB
         with pytest.raises(ValueError):
             s.submit("sedov", _params(256), 10)
+
+
+def test_served_worker_failure_fails_every_request_and_refuses_new_ones(gpu_lib):
+    import time
+    from fv2d_gb300._abi import ERR_CUDA
+    from fv2d_gb300.serve import Server
+    # the budget holds one 128^2 state pair (0.68 MB): one request resident, two queued
+    with Server(budget_bytes=1e6, autotune=False) as s:
+        ids = [s.submit("sedov", _params(128), 1 << 30) for _ in range(3)]
+        deadline = time.time() + 60
+        while time.time() < deadline:
+            st = s.stats()
+            if st.admitted == 1 and st.queued == 2:
+                break
+            time.sleep(0.01)
+        assert st.admitted == 1 and st.queued == 2
+        assert s.last_error() == ""
+        s.inject_fault()
+        assert s.drain(60) == ERR_CUDA
+        res = {r.id: r for r in s.poll()}
+        assert sorted(res) == sorted(ids)
+        assert all(r.status == ERR_CUDA for r in res.values())
+        st = s.stats()
+        assert (st.failed, st.completed, st.active, st.queued) == (3, 0, 0, 0)
+        assert "simulated" in s.last_error()
+        with pytest.raises(RuntimeError):
+            s.submit("sedov", _params(128), 10)
+        with pytest.raises(KeyError):
+            s.get_prim(ids[0])
