@@ -494,8 +494,15 @@ int fv2d_create(const fv2d_params *p, int device, fv2d_ctx **out) {
   if (ctx->U1) cudaMemsetAsync(ctx->U1, 0, bytes, ctx->stream);
 
   // position-only tables, computed on the host like the reference's CPU build
-  std::vector<float> grow(p->Ny);
-  std::vector<double> krow(4 * (size_t)p->Ny);
+  std::vector<float> grow;
+  std::vector<double> krow;
+  try {
+    grow.resize(p->Ny);
+    krow.resize(4 * (size_t)p->Ny);
+  } catch (const std::bad_alloc &) {
+    ctx->err = "host allocation failed";
+    return bail(FV2D_ERR_NOMEM);
+  }
   for (int j = 0; j < p->Ny; ++j) {
     grow[j] = (p->gravity_mode == FV2D_GRAV_ANALYTICAL) ? analytical_gravity_row(*p, j) : 0.0f;
     kappa_row(*p, j, &krow[4 * (size_t)j]);
@@ -577,7 +584,12 @@ int fv2d_init_problem(fv2d_ctx *ctx, int problem) {
   if (!ctx) return FV2D_ERR_INVALID;
   if (!problem_valid(problem)) return fail(ctx, FV2D_ERR_INVALID, "unknown problem id");
   const fv2d_params &p = ctx->p;
-  std::vector<double> q((size_t)p.Nx * p.Ny * 4);
+  std::vector<double> q;
+  try {
+    q.resize((size_t)p.Nx * p.Ny * 4);
+  } catch (const std::bad_alloc &) {
+    return fail(ctx, FV2D_ERR_NOMEM, "host allocation failed");
+  }
   for (int j = 0; j < p.Ny; ++j)
     for (int i = 0; i < p.Nx; ++i) init_cell(p, problem, i, j, &q[((size_t)j * p.Nx + i) * 4]);
   CK(cudaMemcpyAsync(ctx->stage, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
@@ -687,7 +699,7 @@ int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, in
   CK(cudaGetLastError());
   if (int rc = ensure_graph(ctx)) return rc;
   const int G = ctx->graph_steps;
-  int launched = 0;
+  long long launched = 0;  // no overflow for max_steps near INT_MAX
   for (;;) {
     // keep a few replays in flight between status checks
     const int burst = 4;
@@ -718,7 +730,7 @@ int fv2d_run_async(fv2d_ctx *ctx, int n) {
   begin_kernel<<<1, 1, 0, ctx->stream>>>(ctx->st, INFINITY, -1.0, ctx->p.epsilon, 0, 1, n);
   CK(cudaGetLastError());
   if (int rc = ensure_graph(ctx)) return rc;
-  int k = 0;
+  long long k = 0;
   for (; k + ctx->graph_steps <= n; k += ctx->graph_steps) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
   for (; k < n; ++k)
     if (int rc = launch_update(ctx, 1, 0.0)) return rc;
