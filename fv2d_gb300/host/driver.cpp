@@ -87,9 +87,11 @@ int main(int argc, char **argv) {
   if (r.cfg.problem_id < 0) return die(std::string("Error unknown problem ") + r.cfg.problem);  // Init.h:303-304
 
   namespace fs = std::filesystem;
-  if (!fs::exists(r.cfg.output_path)) {  // IOManager.h:84-88
+  std::error_code fs_ec;
+  if (!fs::exists(r.cfg.output_path, fs_ec)) {  // IOManager.h:84-88
     std::cout << "Output path does not exist, creating directory `" << r.cfg.output_path << "`." << std::endl;
-    fs::create_directory(r.cfg.output_path);
+    if (!fs::create_directory(r.cfg.output_path, fs_ec) && fs_ec)
+      return die(std::string("cannot create ") + r.cfg.output_path + ": " + fs_ec.message());
   }
   fv2d_write_ini_echo(argv[1], "last.ini");
   fv2d_write_ini_echo(argv[1], (std::string(r.cfg.output_path) + "/" + r.cfg.output_filename + ".ini").c_str());
@@ -106,7 +108,7 @@ int main(int argc, char **argv) {
     const std::string path = d == std::string::npos ? file : file.substr(0, d + 3);
     const std::string out = std::string(r.cfg.output_path) + "/" + r.cfg.output_filename + ".h5";
     std::error_code ec;
-    if (!r.cfg.multiple_outputs && fs::exists(out) && fs::equivalent(path, out, ec)) {
+    if (!r.cfg.multiple_outputs && fs::exists(out, ec) && fs::equivalent(path, out, ec)) {
       if (d != std::string::npos)
         return die(
             "Invalid restart file : if your restart file and output file are the same, you can only start from the "
@@ -144,8 +146,8 @@ int main(int argc, char **argv) {
   std::vector<double> rec(6 * 4096);
   long long step_no = 0;
   for (;;) {
-    double td;
-    int n, status;
+    double td = t;  // outputs of fv2d_advance, kept defined when it fails before writing them
+    int n = 0, status = FV2D_RUN_NUMERIC;
     const auto w0 = std::chrono::steady_clock::now();
     const int rc = fv2d_advance(r.ctx, 4096, r.p.tend, next_save, resumed_after_save ? 1 : 0, &td, &n, &status);
     const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
@@ -175,8 +177,12 @@ int main(int argc, char **argv) {
     }
     resumed_after_save = false;
     t = td;
+    if (status == FV2D_RUN_NUMERIC || rc != FV2D_OK) {  // also a device error reported with a save stop
+      std::cerr << "stopping: " << fv2d_last_error(r.ctx) << std::endl;
+      break;
+    }
     if (status == FV2D_RUN_SAVE) {  // main.cpp:64-77: dt line, save, then the update
-      double dt, ih, itc_s, iv_s;
+      double dt = 0, ih = 0, itc_s = 0, iv_s = 0;
       fv2d_compute_dt(r.ctx, &dt, &ih, &itc_s, &iv_s);
       if (next_log == 0) print_dt(r, t, ih, itc_s, iv_s);
       next_log = next_log == 0 ? r.p.log_frequency : next_log - 1;
@@ -185,10 +191,6 @@ int main(int argc, char **argv) {
       next_save += r.p.save_freq;
       resumed_after_save = true;
       continue;
-    }
-    if (status == FV2D_RUN_NUMERIC || rc != FV2D_OK) {
-      std::cerr << "stopping: " << fv2d_last_error(r.ctx) << std::endl;
-      break;
     }
     if (status == FV2D_RUN_DONE) break;
   }
