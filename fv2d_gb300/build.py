@@ -59,7 +59,7 @@ DRIVER = os.path.join(PKG, "bin", "fv2d_gpu")
 
 def _headers():
     return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
-        glob.glob(os.path.join(REPO, "include", "*.h"))
+        glob.glob(os.path.join(CSRC, "*.hpp")) + glob.glob(os.path.join(REPO, "include", "*.h"))
 
 
 def _stale(obj, src, hdr_mtime):

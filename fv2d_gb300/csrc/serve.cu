@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "../../include/fv2d_serve.h"
+#include "arena.hpp"
 #include "batch_common.cuh"
 #include "ic.h"
 #include "physics.cuh"
@@ -153,73 +154,17 @@ __global__ void __launch_bounds__(256) cons_kernel(const SimDev *sims, int slot,
 }
 
 // ---------------------------------------------------------------- arena
-struct Arena {
-  struct Chunk {
-    char *base;
-    size_t size;
-    std::map<size_t, size_t> free;  // offset -> size
-  };
-  std::vector<Chunk> chunks;
-  double budget = 0;
-  size_t reserved = 0, in_use = 0;
-
-  static size_t align(size_t n) { return (n + 255) & ~size_t(255); }
-
-  void *alloc(size_t n) {
-    n = align(n);
-    for (auto &c : chunks)
-      for (auto it = c.free.begin(); it != c.free.end(); ++it)
-        if (it->second >= n) {
-          const size_t off = it->first, sz = it->second;
-          c.free.erase(it);
-          if (sz > n) c.free[off + n] = sz - n;
-          in_use += n;
-          return c.base + off;
-        }
-    // grow: chunks of at least 1 GiB, within the budget
-    size_t want = std::max(n, (size_t)1 << 30);
-    if ((double)(reserved + want) > budget) want = n;
-    if ((double)(reserved + want) > budget) return nullptr;
-    char *p = nullptr;
-    if (cudaMalloc(&p, want) != cudaSuccess) {
+// Device memory for the state arena (arena.hpp).
+struct DeviceMemory {
+  static void *reserve(size_t n) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, n) != cudaSuccess) {
       cudaGetLastError();
       return nullptr;
     }
-    Chunk c{p, want, {}};
-    if (want > n) c.free[n] = want - n;
-    chunks.push_back(std::move(c));
-    reserved += want;
-    in_use += n;
     return p;
   }
-  void release(void *ptr, size_t n) {
-    n = align(n);
-    char *p = static_cast<char *>(ptr);
-    for (auto &c : chunks)
-      if (p >= c.base && p < c.base + c.size) {
-        const size_t off = p - c.base;
-        in_use -= n;
-        auto next = c.free.lower_bound(off);
-        if (next != c.free.end() && next->first == off + n) {  // merge with the following block
-          n += next->second;
-          next = c.free.erase(next);
-        }
-        if (next != c.free.begin()) {  // merge with the preceding block
-          auto prev = std::prev(next);
-          if (prev->first + prev->second == off) {
-            prev->second += n;
-            return;
-          }
-        }
-        c.free[off] = n;
-        return;
-      }
-  }
-  void free_all() {
-    for (auto &c : chunks) cudaFree(c.base);
-    chunks.clear();
-    reserved = in_use = 0;
-  }
+  static void unreserve(void *p) { cudaFree(p); }
 };
 
 struct Pending {
@@ -275,7 +220,7 @@ struct fv2d_server {
   double *d_cons = nullptr, *h_cons = nullptr;
   float *h_stage = nullptr;
   size_t h_stage_size = 0;
-  Arena arena;
+  Arena<DeviceMemory> arena;
   // queues
   std::mutex mu;
   std::condition_variable cv;
