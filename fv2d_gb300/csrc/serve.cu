@@ -22,6 +22,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -226,7 +227,7 @@ struct fv2d_server {
   std::condition_variable cv;
   std::deque<Pending> queue;
   std::vector<fv2d_result> done_unpolled;
-  std::unordered_map<int64_t, Finished> finished;
+  std::unordered_map<int64_t, std::shared_ptr<const Finished>> finished;  // shared: get_prim reads outside mu
   int64_t next_id = 1;
   int64_t n_submitted = 0, n_admitted = 0, n_completed = 0, n_failed = 0;
   std::atomic<bool> stop{false};
@@ -679,7 +680,7 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
       s->n_failed++;
     try {
       s->done_unpolled.push_back(r);
-      if (kept) s->finished.emplace(r.id, std::move(fin));
+      if (kept) s->finished.emplace(r.id, std::make_shared<const Finished>(std::move(fin)));
     } catch (const std::bad_alloc &) {  // counted; its record or final state is lost
     }
   }
@@ -1064,10 +1065,14 @@ int fv2d_server_drain(fv2d_server *s, double timeout_s) {
 
 int fv2d_server_get_prim(fv2d_server *s, int64_t id, double *q) {
   if (!s || !q) return FV2D_ERR_INVALID;
-  std::lock_guard<std::mutex> lock(s->mu);
-  auto it = s->finished.find(id);
-  if (it == s->finished.end()) return FV2D_ERR_STATE;
-  const Finished &f = it->second;
+  std::shared_ptr<const Finished> held;  // keeps the state alive through a concurrent release
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->finished.find(id);
+    if (it == s->finished.end()) return FV2D_ERR_STATE;
+    held = it->second;
+  }
+  const Finished &f = *held;
   const int N = f.res.N;
   const size_t n = (size_t)N * N;
   const double gm1 = f.gamma - 1.0;
