@@ -134,3 +134,17 @@ def test_no_cpu_fallback_without_a_gpu(libs):
         return
     s.close()
     pytest.skip("a GPU is present")
+
+
+def test_server_has_no_cpu_fallback_without_a_gpu(libs):
+    """A valid server configuration without a usable GPU: FV2D_ERR_CUDA, no
+    server, no worker thread."""
+    from fv2d_gb300.serve import ServerConfig, _bind
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = _bind(libs)
+    cfg = ServerConfig(C.sizeof(ServerConfig), 0, 1e9, 16, 0, 0, 0, 0.0)
+    h = C.c_void_p()
+    assert lib.fv2d_server_create(C.byref(cfg), C.byref(h)) == _abi.ERR_CUDA
+    assert not h.value
