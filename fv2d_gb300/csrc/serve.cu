@@ -36,6 +36,7 @@
 #include "ic.h"
 #include "physics.cuh"
 #include "problems.h"
+#include "schedule.hpp"
 #include "nvtx_range.h"
 
 namespace fv2d {
@@ -495,23 +496,14 @@ double remaining_work(const fv2d_server *s, int slot) {
 
 void rebuild_lists(fv2d_server *s) {
   std::vector<WorkItem> lists[kBuckets];
-  std::vector<int> run;
+  // shortest remaining work first, up to about active_cells cells per step
+  // (every resident request when active_cells is 0)
+  std::vector<Candidate> cand;
   for (int k = 0; k < s->max_sims; ++k)
-    if (s->slots[k].used) run.push_back(k);
-  if (s->cfg.active_cells > 0) {
-    // shortest remaining work first, up to about active_cells cells per step
-    std::vector<std::pair<double, int>> order;
-    for (int k : run) order.emplace_back(remaining_work(s, k), k);
-    std::sort(order.begin(), order.end());
-    run.clear();
-    double cells = 0;
-    for (const auto &o : order) {
-      if (!run.empty() && cells >= s->cfg.active_cells) break;
-      run.push_back(o.second);
-      cells += (double)s->slots[o.second].req.params.Nx * s->slots[o.second].req.params.Ny;
-    }
-    std::sort(run.begin(), run.end());
-  }
+    if (s->slots[k].used)
+      cand.push_back({k, s->cfg.active_cells > 0 ? remaining_work(s, k) : 0.0,
+                      (double)s->slots[k].req.params.Nx * s->slots[k].req.params.Ny});
+  const std::vector<int> run = select_active(std::move(cand), s->cfg.active_cells);
   // interleave tiles of the simulations of a bucket so that a CTA's
   // consecutive items belong to different simulations
   std::vector<int> per_bucket[kBuckets];
