@@ -349,9 +349,14 @@ int admit(fv2d_server *s, const Pending &pd) {
   int tx, ty, nt, staging;
   batch_cfg_info(s->bucket_cfg[bucket], &tx, &ty, &nt, &staging, nullptr, nullptr);
   const int items = ((N + tx - 1) / tx) * ((N + ty - 1) / ty);
-  if (!reserve_work(s, bucket, s->items_in[bucket] + items)) return -1;
+  // state memory first: a request that does not fit must not grow the work
+  // lists (that synchronises the stream and drops the captured graphs)
   void *mem = s->arena.alloc(bytes);
   if (!mem) return -1;
+  if (!reserve_work(s, bucket, s->items_in[bucket] + items)) {
+    s->arena.release(mem, bytes);
+    return -1;
+  }
   s->items_in[bucket] += items;
   const int slot = s->free_slots.back();
   s->free_slots.pop_back();
