@@ -1038,7 +1038,7 @@ int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id) {
 }
 
 int fv2d_server_poll(fv2d_server *s, fv2d_result *out, int max, int *n) {
-  if (!s || !n || (max > 0 && !out)) return FV2D_ERR_INVALID;
+  if (!s || !n || max < 0 || (max > 0 && !out)) return FV2D_ERR_INVALID;
   std::lock_guard<std::mutex> lock(s->mu);
   const int k = std::min<int>(max, (int)s->done_unpolled.size());
   for (int i = 0; i < k; ++i) out[i] = s->done_unpolled[i];

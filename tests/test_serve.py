@@ -142,6 +142,16 @@ def test_rejects_unsupported_requests(gpu_lib):
                 s.submit("sedov", params(128, **bad), 10)
         with pytest.raises(ValueError):
             s.submit("sedov", params(100), 10)  # not a multiple of 32
+        # argument checks of the C entry points
+        import ctypes as C
+        from fv2d_gb300._abi import ERR_INVALID
+        n = C.c_int(-7)
+        assert s.L.fv2d_server_poll(s.h, None, -1, C.byref(n)) == ERR_INVALID
+        assert s.L.fv2d_server_poll(s.h, None, 4, C.byref(n)) == ERR_INVALID
+        assert s.L.fv2d_server_poll(s.h, None, 0, C.byref(n)) == 0 and n.value == 0
+        assert s.L.fv2d_server_drain(s.h, float("nan")) == ERR_INVALID
+        assert s.L.fv2d_server_drain(s.h, -1.0) == ERR_INVALID
+        assert s.L.fv2d_server_last_error(s.h, None, 16) == ERR_INVALID
 
 
 @pytest.mark.parametrize("active", [0.0, 2e5])
