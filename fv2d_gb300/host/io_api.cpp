@@ -63,35 +63,45 @@ extern "C" {
 
 int fv2d_read_ini(const char *path, fv2d_params *p, fv2d_run_config *run, char *err, int errlen) {
   if (!path || !p || !run) return FV2D_ERR_INVALID;
-  IniFile ini(path);
-  if (ini.error() < 0) {
-    set_err(err, errlen, std::string("cannot open ") + path);
-    return FV2D_ERR_INVALID;
-  }
-  try {
+  return guarded(err, errlen, [&]() -> int {
+    IniFile ini(path);
+    if (ini.error() < 0) {
+      set_err(err, errlen, std::string("cannot open ") + path);
+      return FV2D_ERR_INVALID;
+    }
     ParamReader reader(std::move(ini));
     RunConfig rc;
     read_ini(reader, p, &rc);
     reader.check_validity(std::cerr);
+    // a string that does not fit its fixed field is refused, never cut short
+    // (a shortened output path would write somewhere else)
+    const struct {
+      char *dst;
+      size_t cap;
+      const std::string *src;
+      const char *key;
+    } fields[] = {{run->problem, sizeof run->problem, &rc.problem, "[physics] problem"},
+                  {run->output_filename, sizeof run->output_filename, &rc.filename_out, "[run] output_filename"},
+                  {run->output_path, sizeof run->output_path, &rc.output_path, "[run] output_path"},
+                  {run->restart_file, sizeof run->restart_file, &rc.restart_file, "[run] restart_file"}};
+    for (const auto &f : fields)
+      if (f.src->size() >= f.cap) {
+        set_err(err, errlen, std::string(f.key) + " is longer than " + std::to_string(f.cap - 1) + " bytes");
+        return FV2D_ERR_SIZE;
+      }
     std::memset(run, 0, sizeof(*run));
-    copy_str(run->problem, sizeof run->problem, rc.problem);
-    copy_str(run->output_filename, sizeof run->output_filename, rc.filename_out);
-    copy_str(run->output_path, sizeof run->output_path, rc.output_path);
-    copy_str(run->restart_file, sizeof run->restart_file, rc.restart_file);
+    for (const auto &f : fields) copy_str(f.dst, f.cap, *f.src);
     run->multiple_outputs = rc.multiple_outputs ? 1 : 0;
     run->problem_id = problem_id(rc.problem);
-  } catch (const std::exception &e) {
-    set_err(err, errlen, e.what());
-    return FV2D_ERR_INVALID;
-  }
-  return FV2D_OK;
+    return FV2D_OK;
+  });
 }
 
 int fv2d_write_ini_echo(const char *ini_path, const char *out_path) {
   if (!ini_path || !out_path) return FV2D_ERR_INVALID;
-  IniFile ini(ini_path);
-  if (ini.error() < 0) return FV2D_ERR_INVALID;
-  try {
+  return guarded(nullptr, 0, [&]() -> int {
+    IniFile ini(ini_path);
+    if (ini.error() < 0) return FV2D_ERR_INVALID;
     ParamReader reader(std::move(ini));
     fv2d_params p;
     RunConfig rc;
@@ -99,10 +109,8 @@ int fv2d_write_ini_echo(const char *ini_path, const char *out_path) {
     std::ofstream out(out_path);
     if (!out) return FV2D_ERR_INVALID;
     reader.write_echo(out);
-  } catch (const std::exception &) {
-    return FV2D_ERR_INVALID;
-  }
-  return FV2D_OK;
+    return FV2D_OK;
+  });
 }
 
 int fv2d_snapshot_write(const char *dir, const char *name, int multiple_outputs, int truncate, const fv2d_params *p,

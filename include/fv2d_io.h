@@ -33,8 +33,9 @@ typedef struct fv2d_run_config {
 
 /* Parses an .ini file.  FV2D_ERR_INVALID with a message in err (the
  * reference's exception text) on a bad map-valued parameter or an unreadable
- * file; warnings for unknown sections/keys go to stderr like
- * checkValidityIni (SimInfo.h:501-527). */
+ * file; FV2D_ERR_SIZE when a string value does not fit its field of
+ * fv2d_run_config (it is never cut short); warnings for unknown sections/keys
+ * go to stderr like checkValidityIni (SimInfo.h:501-527). */
 int fv2d_read_ini(const char *path, fv2d_params *p, fv2d_run_config *run, char *err, int errlen);
 
 /* Writes the parameter echo of the .ini at ini_path to out_path. */

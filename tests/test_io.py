@@ -99,6 +99,19 @@ def test_ini_bad_map_value(L, tmp_path):
     assert err.startswith("bad parameter for riemann_solver") and "allowed values: fslp, hll, hllc" in err
 
 
+def test_ini_string_too_long_for_its_field_is_refused(L, tmp_path):
+    f = tmp_path / "long.ini"
+    f.write_text("[run]\noutput_path=" + "d" * 511 + "\n")
+    rc, _, r, _ = read_ini(L, str(f))
+    assert rc == 0 and r.output_path == b"d" * 511  # the longest that fits
+    f.write_text("[run]\noutput_path=" + "d" * 512 + "\n")
+    rc, _, _, err = read_ini(L, str(f))
+    assert rc == fv._abi.ERR_SIZE and err == "[run] output_path is longer than 511 bytes"
+    f.write_text("[run]\nrestart_file=" + "r" * 600 + "\n")
+    rc, _, _, err = read_ini(L, str(f))
+    assert rc == fv._abi.ERR_SIZE and "restart_file" in err
+
+
 REF_DUMP = ["Nx", "Ny", "Nghosts", "xmin", "xmax", "ymin", "ymax", "CFL", "boundary_x", "boundary_y",
             "reconstruction", "riemann_solver", "time_stepping", "tend", "save_freq", "gamma0", "epsilon",
             "epsilon_reset_negative", "well_balanced_flux_at_y_bc", "fslp_K", "seed", "log_frequency", "gravity_mode",
