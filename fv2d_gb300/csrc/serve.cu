@@ -1018,6 +1018,13 @@ int fv2d_server_destroy(fv2d_server *s) {
   return FV2D_OK;
 }
 
+int fv2d_server_check_request(const fv2d_request *req, char *buf, int len) {
+  if (!req || (len > 0 && !buf) || len < 0) return FV2D_ERR_INVALID;
+  const char *why = check_request(*req);
+  if (len > 0) std::snprintf(buf, (size_t)len, "%s", why ? why : "");
+  return why ? FV2D_ERR_UNSUPPORTED : FV2D_OK;
+}
+
 int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id) {
   if (!s || !req || !id) return FV2D_ERR_INVALID;
   if (check_request(*req)) return FV2D_ERR_UNSUPPORTED;

@@ -54,11 +54,20 @@ def _bind(L):
     L.fv2d_server_release.argtypes = [vp, C.c_int64]
     L.fv2d_server_get_stats.argtypes = [vp, C.POINTER(Stats)]
     L.fv2d_server_last_error.argtypes = [vp, C.c_char_p, C.c_int]
+    L.fv2d_server_check_request.argtypes = [C.POINTER(Request), C.c_char_p, C.c_int]
     L.fv2d_server_inject_fault.argtypes = [vp]
     L.fv2d_server_config_name.argtypes = [C.c_int]
     L.fv2d_server_config_name.restype = C.c_char_p
     L._serve_bound = True
     return L
+
+
+def check_request(req):
+    """Why the service would refuse a Request ('' when it accepts it); needs
+    no server or GPU."""
+    buf = C.create_string_buffer(256)
+    _bind(_lib_loader()).fv2d_server_check_request(C.byref(req), buf, len(buf))
+    return buf.value.decode()
 
 
 def config_name(index):
@@ -126,7 +135,8 @@ class Server:
         if rc == ERR_STATE:
             raise RuntimeError(f"the service has stopped: {self.last_error()}")
         if rc != 0:
-            raise ValueError(f"request rejected ({rc})")
+            why = check_request(r)
+            raise ValueError(f"request rejected ({rc}{': ' + why if why else ''})")
         self._n[i.value] = params.Nx
         return i.value
 

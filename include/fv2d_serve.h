@@ -99,7 +99,14 @@ typedef struct fv2d_server_stats {
 int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out);
 int fv2d_server_destroy(fv2d_server *s);
 
-/* Queue a request; returns its id.  Thread-safe. */
+/* The checks fv2d_server_submit makes on a request's own fields, without a
+ * server or a GPU: FV2D_OK, or FV2D_ERR_UNSUPPORTED with the reason written
+ * into buf (len bytes at most, NUL-terminated; "" when accepted). */
+int fv2d_server_check_request(const fv2d_request *req, char *buf, int len);
+
+/* Queue a request; returns its id.  FV2D_ERR_UNSUPPORTED (see
+ * fv2d_server_check_request), FV2D_ERR_SIZE when its state can never fit the
+ * budget, FV2D_ERR_STATE once the service has stopped.  Thread-safe. */
 int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id);
 
 /* Results completed since the last poll (at most max); *n receives the count. */

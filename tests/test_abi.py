@@ -148,3 +148,33 @@ def test_server_has_no_cpu_fallback_without_a_gpu(libs):
     h = C.c_void_p()
     assert lib.fv2d_server_create(C.byref(cfg), C.byref(h)) == _abi.ERR_CUDA
     assert not h.value
+
+
+def test_server_request_checks_without_a_server(libs):
+    """fv2d_server_check_request: the request checks of fv2d_server_submit,
+    with their reasons, callable without a server or a GPU."""
+    import fv2d_gb300 as fv
+    from fv2d_gb300.serve import Request, check_request, _bind
+    lib = _bind(libs)
+
+    def req(**kw):
+        base = dict(Nx=128, Ny=128, reconstruction=fv.PLM, riemann_solver=fv.HLLC)
+        base.update(kw)
+        return Request(C.sizeof(Request), fv.PROBLEMS["sedov"], fv.default_params(**base), 10, 0, 0.0)
+
+    assert check_request(req()) == ""
+    buf = C.create_string_buffer(64)
+    assert lib.fv2d_server_check_request(C.byref(req()), buf, 64) == _abi.OK
+    cases = [(dict(riemann_solver=fv.FSLP), "HLL and HLLC"), (dict(Nx=100, Ny=100), "multiple of 32"),
+             (dict(Ny=96), "square"), (dict(time_stepping=fv.TS_RK2), "Euler"),
+             (dict(reconstruction=fv.MUSCL_HANCOCK), "PCM and PLM")]
+    for kw, why in cases:
+        r = req(**kw)
+        assert lib.fv2d_server_check_request(C.byref(r), buf, 64) == _abi.ERR_UNSUPPORTED, kw
+        assert why in buf.value.decode() and why in check_request(r), (kw, buf.value)
+    bad = req()
+    bad.struct_size -= 8
+    assert "struct_size" in check_request(bad)
+    assert lib.fv2d_server_check_request(None, buf, 64) == _abi.ERR_INVALID
+    assert lib.fv2d_server_check_request(C.byref(req()), None, 0) == _abi.OK
+    assert lib.fv2d_server_check_request(C.byref(req()), buf, -1) == _abi.ERR_INVALID
