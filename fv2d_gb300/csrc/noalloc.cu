@@ -7,7 +7,12 @@
 // front), and loops that cannot afford the device-wide synchronisation an
 // allocation may cause.  They pass their own input and output arrays; the
 // only scratch the reduction needs lives in a fixed array inside this
-// library, allocated once when the library is loaded.
+// library's device code.  CUDA loads a library's device code lazily by default:
+// the first call on a device loads this module there (which may allocate
+// device memory and synchronise, like any first use of a module) and looks up
+// the array's address; every later call allocates nothing.  Callers whose
+// loop must not allocate make one call before it (and before any stream
+// capture).
 //
 // The scratch: one static array of 4096 per-CTA partial maxima plus a
 // completion ticket (32 KB + 256 B, resident on every GPU that loads the
@@ -62,7 +67,7 @@ __device__ __forceinline__ double div_spacing(double x, double d, double inv_d, 
 }
 
 // Same per-cell expression and the same max semantics as the dt reduction of
-// the set-up pass and of the fused step (ComputeDt.h:406-409, 421), so the
+// the set-up pass and of the fused step (ComputeDt.h:31-34, 46-48), so the
 // result is bit-identical to fv2d_compute_dt on the same state.
 __global__ void __launch_bounds__(kThreads) dt_noalloc_kernel(DtArgs a) {
   __shared__ double red[kThreads / 32];
@@ -96,7 +101,7 @@ __global__ void __launch_bounds__(kThreads) dt_noalloc_kernel(DtArgs a) {
   }
   __syncthreads();
   if (!s_last) return;
-  // last CTA: reduce the partials, finish computeDt (ComputeDt.h:439)
+  // last CTA: reduce the partials, finish computeDt (ComputeDt.h:64)
   __threadfence();
   double r = -1.0;
   for (int b = threadIdx.x; b < a.nblocks; b += kThreads) {
@@ -122,7 +127,10 @@ __global__ void __launch_bounds__(kThreads) dt_noalloc_kernel(DtArgs a) {
   }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device and kept
+// for the life of the process.  A device reset (cudaDeviceReset) or a new
+// primary context reloads the module at another address, so the entry point
+// must not be used on a device after it has been reset.
 std::mutex g_mu;
 void *g_scratch_addr[256];
 

@@ -101,7 +101,7 @@ void kappa_row(const fv2d_params &p, int j, double out[4]) {
   out[3] = 0.5 * (kC + kappa_at(p, (int)(y + dy)));
 }
 
-// ComputeDt.h:411-419: state-independent parabolic inverse time steps.
+// ComputeDt.h:36-44: state-independent parabolic inverse time steps.
 void parabolic_inv_dt(const fv2d_params &p, double *inv_tc, double *inv_visc) {
   const double dx = (p.xmax - p.xmin) / p.Nx, dy = (p.ymax - p.ymin) / p.Ny;
   double tc = p.epsilon, visc = p.epsilon;

@@ -66,7 +66,7 @@ struct StepArgs {
   double dx, dy, inv_dx, inv_dy;
   int dx_pow2, dy_pow2;  // 1/dx (1/dy) is exact: divisions become products
   uint64_t rw_dx, rw_dy;  // otherwise quotients by dx (dy) share its reciprocal word
-  double one_over_dx, one_over_dy;  // 1.0/dx, 1.0/dy (Viscosity.h:168-169)
+  double one_over_dx, one_over_dy;  // 1.0/dx, 1.0/dy (Viscosity.h:57-58)
   double gx_dx, gy_dy;  // FSLP gravity terms gx*dx, gy*dy (Update.h:119)
   double gxf, gyf;      // constant gravity narrowed to float (Gravity.h:39)
   double eps_reset;     // epsilon_reset_negative

@@ -11,7 +11,7 @@
 //   4. accumulates the conservative update of each cell in the reference's
 //      order -- x flux divergence, x gravity, y flux divergence, y gravity,
 //      thermal conduction, viscosity (Update.h:158-172, 186-190,
-//      ThermalConduction.h:106, Viscosity.h:223-228) -- and, for the RK2
+//      ThermalConduction.h:106, Viscosity.h:112-117) -- and, for the RK2
 //      corrector, the average with U0 (Update.h:214-220);
 //   5. writes U once, converts to primitives and applies the
 //      negative-density/pressure reset with its counters (SimInfo.h:576-636),
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(NT, step_ctas_per_sm<RECON, RS>(VISC))
       }
     }
   }
-  // viscous face terms (Viscosity.h:148-228), once per face: the two cells of
+  // viscous face terms (Viscosity.h:63-107), once per face: the two cells of
   // a face evaluate the same expressions in the reference, the one on the
   // +side of the face with sign -1, which only negates the products exactly
   if constexpr (VISC) {
@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(NT, step_ctas_per_sm<RECON, RS>(VISC))
       }
       un[3] += mulx<12>(s_tc[0], FRt - FLt) + mulx<12>(s_tc[1], FDt - FUt);
     }
-    // viscosity (Viscosity.h:148-228): the face terms of the face pass, the
+    // viscosity (Viscosity.h:63-107): the face terms of the face pass, the
     // -side face negated, accumulated in the reference's order
     if constexpr (VISC) {
       constexpr int NVX = TY * (TX + 1), NVY = (TY + 1) * TX;
@@ -518,7 +518,7 @@ __global__ void __launch_bounds__(NT, step_ctas_per_sm<RECON, RS>(VISC))
       if (fv_lt0(q.r)) { q.r = a.eps_reset; ++cnt_rho; }
       if (fv_lt0(q.p)) { q.p = a.eps_reset; ++cnt_prs; }
       cnt_nan += (unsigned)fv_isnan(q.r) + (unsigned)fv_isnan(q.u) + (unsigned)fv_isnan(q.v) + (unsigned)fv_isnan(q.p);
-      // inverse hyperbolic dt of the new state (ComputeDt.h:406-409)
+      // inverse hyperbolic dt of the new state (ComputeDt.h:31-34)
       const double cs = sound_speed(q, gas);
       const double ih = ddivc(cs + fabs(q.u), a.dx, a.inv_dx, a.dx_pow2, a.rw_dx) +
                         ddivc(cs + fabs(q.v), a.dy, a.inv_dy, a.dy_pow2, a.rw_dy);

@@ -149,36 +149,47 @@ const char *fv2d_last_error(fv2d_ctx *ctx);
  * shape, threads per block, architecture) into buf. */
 int fv2d_build_info(char *buf, int len);
 
-/* Measured binary64 fused multiply-add throughput of `device` in GFLOP/s
- * (2 flops per DFMA), from a dependent-chain-free DFMA loop timed with CUDA
- * events.  Used to state the FP64 roofline of the step kernel. */
-int fv2d_probe_fp64_peak(int device, double *gflops);
-
 /* Allocation-free CFL time step.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc -- code whose device memory belongs
  * to another allocator (a framework pool that must account for every byte, or
  * a process that reserved all device memory up front) and loops that cannot
  * afford the device-wide synchronisation an allocation may cause.
  *
- * Computes ComputeDtFunctor::computeDt (ComputeDt.h:18-65) of a caller-owned
- * device array q_dev of interleaved interior primitives (Ny x Nx x
- * {rho,u,v,p}, the layout of fv2d_set_prim_device) and writes
+ * Takes a caller-owned device array q_dev of interleaved interior primitives
+ * (Ny x Nx x {rho,u,v,p}, the layout of fv2d_set_prim_device) and writes
  * {dt, inv_dt_hyp, inv_dt_tc, inv_dt_visc} to the caller-owned device array
  * out_dev (4 doubles), queued on `stream` (a cudaStream_t, NULL = default
- * stream); the result equals fv2d_compute_dt's on the same state bit for bit.
+ * stream); the result equals fv2d_compute_dt's on the same state bit for bit
+ * (NaN cells included: like fv2d_compute_dt it skips them).
  * It allocates nothing: its only scratch is a fixed array inside the library
  * (32 KB + 256 B on every GPU that loads the library, held until exit), which
  * limits the grid to FV2D_NOALLOC_MAX_CELLS cells; larger grids return
- * FV2D_ERR_SIZE before any GPU work.  The first call on a device looks up the
- * array's device address with that device current; make that first call
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU (other streams, other host threads) race -- serialise
- * them. */
+ * FV2D_ERR_SIZE before any GPU work.  The first call on a device loads the
+ * library's device code there if nothing has yet (CUDA loads modules lazily;
+ * that load may allocate and synchronise) and looks up the array's device
+ * address with that device current; later calls allocate nothing.  Make that
+ * first call before the loop that must not allocate and before any stream
+ * capture, and do not call it on a device after cudaDeviceReset.  All calls
+ * share the array: calls whose work overlaps on the GPU (other streams, other
+ * host threads) race -- serialise them. */
 #define FV2D_NOALLOC_CELLS_PER_BLOCK 4096
 #define FV2D_NOALLOC_MAX_CELLS (4096 * 4096)
 int fv2d_compute_dt_noalloc(const fv2d_params *p, const double *q_dev, double *out_dev, void *stream);
 
-/* Self-test of the step kernel's binary64 arithmetic on the integer pipes:
+/* ------------------------------------------------------------------------
+ * Measurement and test hooks.  Not part of the drop-in interface: nothing in
+ * the step or the service calls them; the benchmark and the tests use them to
+ * state the FP64 roofline and to check the device arithmetic and the bounded
+ * waits on the GPU that runs the library.
+ * ------------------------------------------------------------------------ */
+
+/* Measurement hook: measured binary64 fused multiply-add throughput of
+ * `device` in GFLOP/s (2 flops per DFMA), from a dependent-chain-free DFMA
+ * loop timed with CUDA events.  Used to state the FP64 roofline of the step
+ * kernel. */
+int fv2d_probe_fp64_peak(int device, double *gflops);
+
+/* Test hook: self-test of the step kernel's binary64 arithmetic on the integer pipes:
  * op 0 = division, 1 = square root, 2 = comparisons, 3 = fmax / fmin,
  * 4 = scalings by powers of two, 5 = multiplication.  Evaluates n generated operand sets
  * (random significands, arbitrary bit patterns, near-tie and exact cases,
@@ -187,7 +198,7 @@ int fv2d_compute_dt_noalloc(const fv2d_params *p, const double *q_dev, double *o
  * example receives {a, b, integer result} of the first mismatch. */
 int fv2d_selftest_arith(int op, uint64_t n, uint64_t seed, uint64_t *mismatches, double example[3]);
 
-/* Self-test of the device-side wait guard (no reference counterpart): one
+/* Test hook: self-test of the device-side wait guard (no reference counterpart): one
  * thread waits, with the step kernel's bounded wait and an iteration limit of
  * `limit` (1 .. 2^20), on a barrier that is never completed.  *timed_out
  * receives the error bits the wait sets (DEVERR_TMA_TIMEOUT = 1) instead of

@@ -1,14 +1,15 @@
 #!/bin/sh
 # Builds oracle/_ref/libfv2d_ref.so from the reference's own headers, compiled
-# in place from the reference checkout (REF_DIR, default /root/reference)
-# against the serial stand-ins in oracle/ref_check/include.  Test
-# infrastructure only: used to pin the oracle and to generate the fixtures
-# under tests/golden/.  Outputs go to oracle/_ref/ only.
+# in place from REF_DIR (default: baseline/_ref, where oracle/ref_check/stage.sh
+# puts them) against the serial stand-ins in oracle/ref_check/include.  Test
+# infrastructure only: used to pin the oracle, to generate the fixtures under
+# tests/golden/ and to time the reference's own step code on the host cores.
+# Outputs go to oracle/_ref/ only.  Exits 2 when REF_DIR holds no reference.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_DIR="${REF_DIR:-/root/reference}"
+REF_DIR="${REF_DIR:-$HERE/../../baseline/_ref}"
 OUT="$HERE/../_ref"
-[ -f "$REF_DIR/Update.h" ] || { echo "reference checkout not found at $REF_DIR" >&2; exit 2; }
+[ -f "$REF_DIR/Update.h" ] || { echo "reference sources not found at $REF_DIR" >&2; exit 2; }
 mkdir -p "$OUT"
 ${CXX:-g++} -std=c++20 -O2 -ffp-contract=off -fPIC -shared -w \
   -I"$HERE/include" -I"$REF_DIR" \

@@ -1,7 +1,7 @@
 """The .ini parameters and HDF5 snapshot layout (include/fv2d_io.h), no GPU.
 
 * .ini: inih line rules, the Reader's float rounding, map-valued errors; and,
-  where the reference checkout is present, every settings/*.ini read by this
+  where the reference's sources are staged, every settings/*.ini read by this
   library equals the reference's own readInifile result (all parameters) and
   the echoed parameter file is byte-identical to Reader::outputValues.
 * HDF5: snapshots written by the library are read back by its own reader and
@@ -20,7 +20,9 @@ from fv2d_gb300._abi import Params
 from fv2d_testlib import ref_available, ref_lib
 from h5lite import H5
 
-REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+# the reference's sources as staged for the cross-check build (oracle/ref_check/stage.sh)
+REF_DIR = os.environ.get("REF_DIR",
+                         os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "baseline", "_ref"))
 
 
 class RunConfig(C.Structure):

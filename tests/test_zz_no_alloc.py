@@ -15,7 +15,7 @@ collected last on purpose.
 import numpy as np
 import pytest
 
-from fv2d_testlib import bits_equal, random_prim, reference_params
+from fv2d_testlib import Oracle, bits_equal, random_prim, reference_params
 
 pytestmark = pytest.mark.gpu
 
@@ -51,6 +51,32 @@ def test_noalloc_dt_matches_compute_dt_twice(gpu_lib):
     stream.synchronize()
     assert bits_equal(out.cpu().numpy(), expect2)
     assert not bits_equal(expect1, expect2)
+
+
+def test_noalloc_dt_skips_a_nan_cell_like_compute_dt(gpu_lib):
+    """A state with one NaN cell: the reference's max reduction (fmax,
+    ComputeDt.h:46-48) skips it, and so do both entry points -- same bits,
+    also against the oracle."""
+    import torch
+    import fv2d_gb300 as fv
+
+    p = reference_params(Nx=96, Ny=80, gamma0=1.4, CFL=0.8)
+    q = random_prim(80, 96, 5)
+    q[17, 41, 3] = np.nan  # a NaN pressure: its sound speed and inverse dt are NaN
+    s = fv.Simulation(p)
+    s.set_prim(q)
+    expect = np.array(s.compute_dt())
+    o = Oracle(p)
+    o.set_prim(q)
+    assert bits_equal(expect, o.compute_dt())
+    assert np.all(np.isfinite(expect))
+    qd = torch.from_numpy(s.get_prim()).to("cuda")
+    assert bool(torch.isnan(qd).any())
+    out = torch.full((4,), -7.0, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    assert fv.compute_dt_noalloc(p, qd.data_ptr(), out.data_ptr(), stream.cuda_stream) == 0
+    stream.synchronize()
+    assert bits_equal(out.cpu().numpy(), expect)
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch(gpu_lib):
