@@ -96,11 +96,13 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
       __syncthreads();
       continue;
     }
-    const int N = S.N, P = S.pitch;
+    const int Nx = S.Nx, Ny = S.Ny, P = S.pitch;
     const long long PL = S.plane;
     const int cur = S.cur;
-    const float *src = S.U[cur];
-    float *dst = S.U[1 - cur];
+    const StageBuffers B = stage_buffers(S.U, cur, S.ts, S.stage);
+    const float *src = B.src;
+    float *dst = B.dst;
+    const int sbuf = (B.src == S.U[cur]) ? cur : 1 - cur;  // the buffer staged by TMA
     const int i0 = item.tx * TX, j0 = item.ty * TY;
     const float dt = (float)S.dt;
     const Gas<float> gas{S.gamma, S.gm1, S.entho, 1.1f};
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
     // ---- stage the conservative tile + halo -----------------------------
     if (STAGING == 1 && S.tma_ok) {
       if (tid == 0) {
-        const CUtensorMap *tm = a.tmaps + 2 * item.sim + cur;
+        const CUtensorMap *tm = a.tmaps + 2 * item.sim + sbuf;
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(tm))
                      : "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bk::smem_u32(&mbar)),
@@ -120,9 +122,21 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
             "l"(reinterpret_cast<uint64_t>(tm)), "r"(i0), "r"(j0), "r"(0), "r"(bk::smem_u32(&mbar))
             : "memory");
       }
-      uint32_t it = 0;
-      while (!bk::mbar_try_wait(&mbar, phase))
-        if (++it > (1u << 24)) break;  // bounded: a lost load leaves the tile unchanged, never hangs
+      // bounded wait; a copy that outlives it fails this simulation (its
+      // commit reads dev_err) and is waited for once more, bounded, before
+      // the tile buffer is used again; one that outlives that too stops the
+      // CTA and raises the launch's fault flag, which stops the service
+      bool ok = false;
+      const uint32_t limit = *(volatile unsigned int *)(a.ctl + 1);
+      for (uint32_t it = 0; it < limit && !ok; ++it) ok = bk::mbar_try_wait(&mbar, phase);
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) atomicOr(&a.sims[item.sim].dev_err, (unsigned)BATCH_ERR_TMA_TIMEOUT);
+        for (uint32_t it = 0; it < kTileWaitFinal && !ok; ++it) ok = bk::mbar_try_wait(&mbar, phase);
+        if (__syncthreads_or(!ok)) {
+          if (tid == 0) atomicOr(a.ctl, (unsigned)BATCH_ERR_TMA_TIMEOUT);
+          return;
+        }
+      }
       phase ^= 1u;
     } else {
       constexpr int PER = SH * SW;
@@ -131,20 +145,23 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
         const int ly = r / SW, lx = r % SW;
         const int gy = j0 + ly, gx = i0 + lx;  // padded coordinates
         float v = 0.f;
-        if (gx < N + 4 && gy < N + 4) v = __ldg(src + k * PL + (long long)gy * P + gx);
+        if (gx < Nx + 4 && gy < Ny + 4) v = __ldg(src + k * PL + (long long)gy * P + gx);
         sm[L::Q + e] = v;
       }
     }
     __syncthreads();
 
-    // ---- conservative -> primitive in place, negative reset ---------------
+    // ---- conservative offsets -> primitive in place, negative reset except
+    //      in the second RK2 stage (whose Q is consToPrim(U*) alone) ---------
     for (int e = tid; e < SH * SW; e += NT) {
       const int ly = e / SW, lx = e % SW;
-      float r = sQ(0, ly, lx), mu = sQ(1, ly, lx), mv = sQ(2, ly, lx), E = sQ(3, ly, lx);
+      float r = sQ(0, ly, lx) + S.bg_r, mu = sQ(1, ly, lx), mv = sQ(2, ly, lx), dE = sQ(3, ly, lx);
       float u = mu / r, v = mv / r;
-      float p = pressure_of(E, r, u, v, S.gm1, S.lowmach);
-      if (r < 0.f) r = 1e-8f;
-      if (p < 0.f) p = 1e-8f;
+      float p = pressure_of(dE, S.bg_e, r, u, v, S.gm1, S.lowmach);
+      if (!B.avg) {
+        if (r < 0.f) r = 1e-8f;
+        if (p < 0.f) p = 1e-8f;
+      }
       sQ(0, ly, lx) = r;
       sQ(1, ly, lx) = u;
       sQ(2, ly, lx) = v;
@@ -235,7 +252,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
     for (int cidx = tid; cidx < TX * TY; cidx += NT) {
       const int ry = cidx / TX, rx = cidx % TX;
       const int i = i0 + rx, j = j0 + ry;
-      if (i >= N || j >= N) continue;
+      if (i >= Nx || j >= Ny) continue;
       const int ly = ry + 2, lx = rx + 2;
       const long long g = (long long)(j + 2) * P + (i + 2);
       float un[4];
@@ -298,27 +315,35 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
         }
         un[1] += f1 * dt; un[2] += f2 * dt; un[3] += f3 * dt;
       }
+      if (B.avg) {  // SSP-RK2: 0.5 (U^n + U**) (Update.h:214-220), offsets alike
+#pragma unroll
+        for (int k = 0; k < 4; ++k) un[k] = 0.5f * (dst[k * PL + g] + un[k]);
+      }
 #pragma unroll
       for (int k = 0; k < 4; ++k) dst[k * PL + g] = un[k];
-      // primitive state of the new cell for the next dt
-      float r = un[0], u = un[1] / r, v = un[2] / r;
-      float p = pressure_of(un[3], r, u, v, S.gm1, S.lowmach);
-      nnan += is_nan_f(r) | is_nan_f(u) | is_nan_f(v) | is_nan_f(p);
-      nneg += (r < 0.f) + (p < 0.f);
-      if (r < 0.f) r = 1e-8f;
-      if (p < 0.f) p = 1e-8f;
-      const float cs = sqrtf(p * S.gamma / r);
-      const float ih = (cs + fabsf(u)) * S.inv_dx + (cs + fabsf(v)) * S.inv_dy;
-      if (ih > lmax) lmax = ih;  // NaN never enters
+      if (B.last) {
+        // primitive state of the new cell for the next dt
+        float r = un[0] + S.bg_r, u = un[1] / r, v = un[2] / r;
+        float p = pressure_of(un[3], S.bg_e, r, u, v, S.gm1, S.lowmach);
+        nnan += is_nan_f(r) | is_nan_f(u) | is_nan_f(v) | is_nan_f(p);
+        nneg += (r < 0.f) + (p < 0.f);
+        if (r < 0.f) r = 1e-8f;
+        if (p < 0.f) p = 1e-8f;
+        const float cs = sqrtf(p * S.gamma / r);
+        const float ih = (cs + fabsf(u)) * S.inv_dx + (cs + fabsf(v)) * S.inv_dy;
+        if (ih > lmax) lmax = ih;  // NaN never enters
+      } else {
+        nnan += is_nan_f(un[0]) | is_nan_f(un[1]) | is_nan_f(un[2]) | is_nan_f(un[3]);
+      }
       // ghost copies (BoundaryConditions.h:82-147, inverse map)
-      const bool ex = (i < 2 || i >= N - 2), ey = (j < 2 || j >= N - 2);
+      const bool ex = (i < 2 || i >= Nx - 2), ey = (j < 2 || j >= Ny - 2);
       if (ex || ey) {
         int tx[5], ty[5];
         bool nx[5], ny[5];
         tx[0] = i; nx[0] = false;
         ty[0] = j; ny[0] = false;
-        const int cx = 1 + (ex ? ghost_targets(i, N, S.bcx, tx + 1, nx + 1) : 0);
-        const int cy = 1 + (ey ? ghost_targets(j, N, S.bcy, ty + 1, ny + 1) : 0);
+        const int cx = 1 + (ex ? ghost_targets(i, Nx, S.bcx, tx + 1, nx + 1) : 0);
+        const int cy = 1 + (ey ? ghost_targets(j, Ny, S.bcy, ty + 1, ny + 1) : 0);
         for (int b = 0; b < cy; ++b)
           for (int c = 0; c < cx; ++c) {
             if (b == 0 && c == 0) continue;
@@ -350,7 +375,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
         nn += red_nan[k];
       }
       SimDev *G = &a.sims[item.sim];
-      atomicMax(&G->acc_bits, __float_as_uint(m));
+      if (B.last) atomicMax(&G->acc_bits, __float_as_uint(m));
       if (n) atomicAdd(&G->negatives, (unsigned long long)n);
       if (nn) atomicAdd(&G->nan_cells, nn);
       __threadfence();
@@ -358,32 +383,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const BatchArgs a) {
       s_last = (t == (unsigned)(S.ntx * S.nty) - 1u);
     }
     __syncthreads();
-    if (s_last && tid == 0) {
-      // commit this simulation's step (ComputeDt.h:64, main.cpp:62, 83)
-      __threadfence();
-      volatile SimDev *G = &a.sims[item.sim];
-      const double ih = (double)__uint_as_float(atomicAdd(&a.sims[item.sim].acc_bits, 0u));
-      double m = ih;
-      if (m < S.inv_tc) m = S.inv_tc;
-      if (m < S.inv_visc) m = S.inv_visc;
-      const double dtn = S.cfl / m;
-      const double t = S.t + S.dt;
-      const int step = S.step + 1;
-      G->t = t;
-      G->step = step;
-      G->cur = 1 - cur;
-      G->dt = dtn;
-      G->acc_bits = 0u;
-      int status = SIM_ACTIVE;
-      if (!(dtn > 0.0) || isinf(dtn) || G->nan_cells)  // the NaN / dt guard fails this request only
-        status = SIM_FAILED;
-      else if (step >= S.max_steps || !(t + S.eps < S.tend))
-        status = SIM_DONE;
-      G->status = status;
-      G->nan_cells = 0u;
-      __threadfence();
-      G->ticket = 0u;
-    }
+    if (s_last && tid == 0) commit_stage(&a.sims[item.sim]);  // ComputeDt.h:64, main.cpp:62, 83
     __syncthreads();
   }
 }

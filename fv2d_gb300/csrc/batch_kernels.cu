@@ -9,19 +9,23 @@ namespace fv2d {
 
 struct BatchCfg {
   int tx, ty, nt, staging;
+  int ext;  // 1: the extended family (batch_march_ext_kernel)
   const char *name;
   size_t smem;
   const void *fn;
 };
 
 #define FV2D_CFG(TX, TY, NT, ST, NAME) \
-  {TX, TY, NT, ST, NAME, BatchSmem<TX, TY>::BYTES, (const void *)batch_step_kernel<TX, TY, NT, ST>}
+  {TX, TY, NT, ST, 0, NAME, BatchSmem<TX, TY>::BYTES, (const void *)batch_step_kernel<TX, TY, NT, ST>}
 
 // Column-marching configurations (batch_march.cuh): 28 interior columns per
 // warp, H rows per work item, no shared memory (staging code 2).
 // MINB caps the registers so that MINB CTAs fit on an SM.
 #define FV2D_MARCH(H, NT, MINB, NAME) \
-  {bm::STRIP, H, NT, 2, NAME, 0, (const void *)batch_march_kernel<H, NT, MINB>}
+  {bm::STRIP, H, NT, 2, 0, NAME, 0, (const void *)batch_march_kernel<H, NT, MINB>}
+// The extended family (FSLP, MUSCL-Hancock, per-row tables, boundary fluxes).
+#define FV2D_MARCH_EXT(H, NT, MINB, NAME) \
+  {bm::STRIP, H, NT, 2, 1, NAME, 0, (const void *)batch_march_ext_kernel<H, NT, MINB>}
 
 static const BatchCfg kCfgs[] = {
     FV2D_CFG(32, 8, 128, 0, "32x8/128/ldg"),
@@ -42,6 +46,8 @@ static const BatchCfg kCfgs[] = {
     FV2D_MARCH(32, 32, 16, "28x32/32/march"),
     FV2D_MARCH(32, 64, 10, "28x32/64x10/march"),
     FV2D_MARCH(32, 32, 20, "28x32/32x20/march"),
+    FV2D_MARCH_EXT(32, 64, 8, "28x32/64/march-ext"),
+    FV2D_MARCH_EXT(16, 64, 8, "28x16/64/march-ext"),
 };
 
 // the service sizes its per-configuration tables for at most 32 entries
@@ -49,8 +55,9 @@ static_assert(sizeof(kCfgs) / sizeof(kCfgs[0]) <= 32, "more tile configurations 
 
 int batch_num_cfgs() { return (int)(sizeof(kCfgs) / sizeof(kCfgs[0])); }
 
-void batch_cfg_info(int i, int *tx, int *ty, int *nt, int *staging, size_t *smem, const char **name) {
+void batch_cfg_info(int i, int *tx, int *ty, int *nt, int *staging, size_t *smem, const char **name, int *ext) {
   const BatchCfg &c = kCfgs[i];
+  if (ext) *ext = c.ext;
   if (tx) *tx = c.tx;
   if (ty) *ty = c.ty;
   if (nt) *nt = c.nt;

@@ -8,9 +8,20 @@
 // from the window.  Every face is solved once (x faces in the lane on their
 // right, y faces as the march crosses them), so the step needs no shared
 // memory, no barriers and little index arithmetic.  Same physics and update
-// order as batch_kernel.cuh (States.h:32-43, RiemannSolvers.h:7-128,
+// order as the reference (States.h:32-43, RiemannSolvers.h:7-171,
 // Update.h:93-174, ThermalConduction.h:36-108, Viscosity.h:27-119), and the
 // same per-simulation commit of the step (ComputeDt.h:64, main.cpp:62-83).
+//
+// Two families of item bodies, each compiled per Riemann solver and
+// reconstruction so that the row loop carries neither branch:
+//   - the common one (batch_march_kernel): HLL or HLLC, PCM or PLM, constant
+//     gravity, constant conductivity, viscosity;
+//   - the extended one (batch_march_ext_kernel): also FSLP and the
+//     MUSCL-Hancock predictor, gravity and conductivity from per-row tables
+//     (analytical gravity, B02 conductivity), the y-boundary conduction
+//     modes and the well-balanced y-boundary flux.
+// Both take SSP-RK2 as two launches (stage_buffers) and store the state as
+// offsets from the simulation's background density and energy.
 #pragma once
 
 #include "batch_common.cuh"
@@ -36,89 +47,116 @@ __device__ __forceinline__ S4<float> add4(const S4<float> &a, const S4<float> &b
 __device__ __forceinline__ S4<float> sub4(const S4<float> &a, const S4<float> &b) {
   return S4<float>{a.r - b.r, a.u - b.u, a.v - b.v, a.p - b.p};
 }
-// half minmod slope of the middle state
+__device__ __forceinline__ S4<float> twice4(const S4<float> &a) {
+  return S4<float>{2.f * a.r, 2.f * a.u, 2.f * a.v, 2.f * a.p};
+}
+// half minmod slope of the middle state (Update.h:59-91 times 0.5)
 __device__ __forceinline__ S4<float> half_slope(const S4<float> &m, const S4<float> &c, const S4<float> &p) {
   return S4<float>{minmod(c.r - m.r, p.r - c.r) * 0.5f, minmod(c.u - m.u, p.u - c.u) * 0.5f,
                    minmod(c.v - m.v, p.v - c.v) * 0.5f, minmod(c.p - m.p, p.p - c.p) * 0.5f};
 }
+__device__ __forceinline__ S4<float> swap_uv(const S4<float> &q) { return S4<float>{q.r, q.v, q.u, q.p}; }
 
 struct SimView {
   const float *src;
   float *dst;
+  const float *rows;
   long long PL;
-  int N, P, cur;
-  float dt, gamma, gm1, entho, inv_dx, inv_dy, gx, gy, kappa, mu;
-  int rs, plm, bcx, bcy, grav, tc, visc, lowmach;
+  int Nx, Ny, P;
+  bool avg, last;
+  float dt, gamma, gm1, inv_dx, inv_dy, dy, gx, gy, kappa, mu, gdx, gdy, bg_r, bg_e;
+  float bctc_lo_v, bctc_hi_v;
+  int bcx, bcy, grav, tc, visc, lowmach, wb, bctc_lo, bctc_hi;
 };
 
-// consToPrim with the negative reset (States.h:32-43, SimInfo.h:618-627)
+// consToPrim of a stored offset state (States.h:32-43); the negative reset of
+// checkNegatives (SimInfo.h:618-627) where the reference's Q carries it: every
+// stage but the second RK2 stage, whose Q is consToPrim(U*) alone
+// (Update.h:209).
 __device__ __forceinline__ S4<float> to_prim(const float u[4], const SimView &S) {
-  float r = u[0];
+  float r = u[0] + S.bg_r;
   const float uu = u[1] / r, vv = u[2] / r;
-  float p = pressure_of(u[3], r, uu, vv, S.gm1, S.lowmach);
-  if (r < 0.f) r = 1e-8f;
-  if (p < 0.f) p = 1e-8f;
+  float p = pressure_of(u[3], S.bg_e, r, uu, vv, S.gm1, S.lowmach);
+  if (!S.avg) {
+    if (r < 0.f) r = 1e-8f;
+    if (p < 0.f) p = 1e-8f;
+  }
   return S4<float>{r, uu, vv, p};
 }
 
 template <int RS>
-__device__ __forceinline__ void solve(const S4<float> &qL, const S4<float> &qR, S4<float> &f, const Gas<float> &gas) {
-  float pout;
-  if constexpr (RS == RS_HLL)
-    riemann_hll(qL, qR, f, pout, gas);
-  else
-    riemann_hllc(qL, qR, f, pout, gas);
+__device__ __forceinline__ S4<float> solve(const S4<float> &qL, const S4<float> &qR, float gdx, const Gas<float> &gas,
+                                           float &pout) {
+  S4<float> f;
+  riemann<RS>(qL, qR, f, pout, gdx, gas);
+  return f;
 }
 
 // y face between a cell and the one below it (swap_component, States.h:104-110)
 template <int RS>
-__device__ __forceinline__ S4<float> yflux(const S4<float> &top, const S4<float> &bottom, const Gas<float> &gas) {
-  S4<float> f;
-  solve<RS>(S4<float>{top.r, top.v, top.u, top.p}, S4<float>{bottom.r, bottom.v, bottom.u, bottom.p}, f, gas);
-  return S4<float>{f.r, f.v, f.u, f.p};
+__device__ __forceinline__ S4<float> yflux(const S4<float> &top, const S4<float> &bottom, float gdy,
+                                           const Gas<float> &gas, float &pout) {
+  return swap_uv(solve<RS>(swap_uv(top), swap_uv(bottom), gdy, gas, pout));
 }
 
 }  // namespace bm
 
-// One work item (see the header comment), with the Riemann solver and the
-// reconstruction fixed at compile time: the kernel dispatches on them once per
-// item, so the row loop carries neither branch.
-template <int H, int RS, bool PLM>
+// One work item (see the header comment), with the Riemann solver, the
+// reconstruction and the family fixed at compile time.
+template <int H, int RS, int RECON, bool EXT>
 __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem item, const volatile SimDev *G,
                                            const int lane) {
   using namespace bm;
+  constexpr bool SLOPES = RECON != BR_PCM;
+  constexpr bool MH = RECON == BR_MH;
+  static_assert(EXT || (RS != RS_FSLP && !MH), "FSLP and MUSCL-Hancock are compiled in the extended family");
   SimView S;
-  S.cur = G->cur;
-  S.src = const_cast<const float *>(G->U[S.cur]);
-  S.dst = const_cast<float *>(G->U[1 - S.cur]);
+  {
+    float *U[2] = {G->U[0], G->U[1]};
+    const StageBuffers B = stage_buffers(U, G->cur, G->ts, G->stage);
+    S.src = B.src;
+    S.dst = B.dst;
+    S.avg = B.avg;
+    S.last = B.last;
+  }
+  S.rows = G->rows;
   S.PL = G->plane;
-  S.N = G->N;
+  S.Nx = G->Nx;
+  S.Ny = G->Ny;
   S.P = G->pitch;
   S.dt = (float)G->dt;
   S.gamma = G->gamma;
   S.gm1 = G->gm1;
-  S.entho = G->entho;
   S.inv_dx = G->inv_dx;
   S.inv_dy = G->inv_dy;
+  S.dy = G->dy;
   S.gx = G->gx;
   S.gy = G->gy;
   S.kappa = G->kappa;
   S.mu = G->mu;
-  S.rs = RS;
-  S.plm = PLM;
+  S.gdx = G->gdx;
+  S.gdy = G->gdy;
+  S.bg_r = G->bg_r;
+  S.bg_e = G->bg_e;
+  S.bctc_lo_v = G->bctc_lo_v;
+  S.bctc_hi_v = G->bctc_hi_v;
   S.bcx = G->bcx;
   S.bcy = G->bcy;
   S.grav = G->grav;
   S.tc = G->tc;
   S.visc = G->visc;
   S.lowmach = G->lowmach;
-  const Gas<float> gas{S.gamma, S.gm1, S.entho, 1.1f};
-  const int N = S.N;
+  S.wb = G->wb;
+  S.bctc_lo = G->bctc_lo;
+  S.bctc_hi = G->bctc_hi;
+  const Gas<float> gas{G->gamma, G->gm1, G->entho, G->fslp_K};
+  const int Nx = S.Nx, Ny = S.Ny;
   const int gxl = item.tx * STRIP + lane;           // padded column of this lane
-  const bool colok = gxl < N + 4;
-  const bool out_lane = lane >= 2 && lane < 30 && gxl - 2 < N;
-  const int j0 = item.ty * H, jend = min(j0 + H, N);  // interior rows [j0, jend)
+  const bool colok = gxl < Nx + 4;
+  const bool out_lane = lane >= 2 && lane < 30 && gxl - 2 < Nx;
+  const int j0 = item.ty * H, jend = min(j0 + H, Ny);  // interior rows [j0, jend)
   const float dtdx = S.dt * S.inv_dx, dtdy = S.dt * S.inv_dy;
+  const float ax = 0.5f * S.dt * S.inv_dx, ay = 0.5f * S.dt * S.inv_dy;  // MUSCL-Hancock half step
 
   auto load = [&](int L, float u[4]) {  // padded row L
     const long long g = (long long)L * S.P + gxl;
@@ -130,8 +168,18 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
     }
   };
   auto yslope = [&](const S4<float> &m, const S4<float> &c, const S4<float> &p) {
-    if constexpr (PLM) return half_slope(m, c, p);
+    if constexpr (SLOPES) return half_slope(m, c, p);
     else return S4<float>{0.f, 0.f, 0.f, 0.f};
+  };
+  auto xslope = [&](const S4<float> &c) {
+    if constexpr (SLOPES) return half_slope(shfl_up4(c, 1), c, shfl_down4(c, 1));
+    else return S4<float>{0.f, 0.f, 0.f, 0.f};
+  };
+  // the state the faces of a cell are reconstructed from: the cell itself,
+  // or its MUSCL-Hancock predictor (full slopes are twice the half slopes)
+  auto predict = [&](const S4<float> &q, const S4<float> &hx, const S4<float> &hy) {
+    if constexpr (MH) return hancock(q, twice4(hx), twice4(hy), ax, ay, S.gamma);
+    else return q;
   };
 
   // prologue: rows j0 .. j0+3 (padded) -> window for output row C = j0 + 2
@@ -146,7 +194,15 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
   S4<float> qp = to_prim(Up, S);
   const S4<float> hm = yslope(qa, qm, q0);
   S4<float> h0 = yslope(qm, q0, qp);
-  S4<float> Gm = yflux<RS>(add4(qm, hm), sub4(q0, h0), gas);
+  S4<float> hx0{0.f, 0.f, 0.f, 0.f};
+  S4<float> qtm = qm;
+  if constexpr (MH) {
+    hx0 = xslope(q0);
+    qtm = predict(qm, xslope(qm), hm);
+  }
+  S4<float> qt0 = predict(q0, hx0, h0);
+  float poutM;
+  S4<float> Gm = yflux<RS>(add4(qtm, hm), sub4(qt0, h0), S.gdy, gas, poutM);
 
   float lmax = 0.f;
   unsigned nneg = 0, nnan = 0;
@@ -155,19 +211,40 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
   float Unext[4];
   load(j0 + 4, Unext);
   for (int C = j0 + 2; C < jend + 2; ++C) {
+    const int j = C - 2;
     float Un[4] = {Unext[0], Unext[1], Unext[2], Unext[3]};
     if (C <= jend) load(C + 3, Unext);
     const S4<float> qn = to_prim(Un, S);
     const S4<float> hp = yslope(q0, qp, qn);
-    const S4<float> Gp = yflux<RS>(add4(q0, h0), sub4(qp, hp), gas);
+    S4<float> hxp{0.f, 0.f, 0.f, 0.f};
+    if constexpr (MH) hxp = xslope(qp);
+    const S4<float> qtp = predict(qp, hxp, hp);
+    float poutP;
+    const S4<float> Gp = yflux<RS>(add4(qt0, h0), sub4(qtp, hp), S.gdy, gas, poutP);
 
     // x faces of row C: lane l solves face l - 1/2
-    const S4<float> qW = shfl_up4(q0, 1), qE = shfl_down4(q0, 1);
-    S4<float> hx{0.f, 0.f, 0.f, 0.f};
-    if constexpr (PLM) hx = half_slope(qW, q0, qE);
-    S4<float> Fw;
-    solve<RS>(shfl_up4(add4(q0, hx), 1), sub4(q0, hx), Fw, gas);
+    S4<float> hx;
+    if constexpr (MH) hx = hx0;
+    else hx = xslope(q0);
+    float poutX;
+    const S4<float> Fw = solve<RS>(shfl_up4(add4(qt0, hx), 1), sub4(qt0, hx), S.gdx, gas, poutX);
     const S4<float> Fe = shfl_down4(Fw, 1);
+
+    // gravity of the row: constant, or the per-row table (the analytical
+    // value applies to both directions, Gravity.h:45-58)
+    float g_x = S.gx, g_y = S.gy;
+    if constexpr (EXT) {
+      if (S.grav == BG_ROW) g_x = g_y = S.rows[j * kRowStride + ROW_G];
+    }
+    // well-balanced y fluxes at the y boundaries (Update.h:149-156)
+    S4<float> GmU = Gm, GpU = Gp;
+    if constexpr (EXT) {
+      if (S.wb) {
+        const float g = S.grav == BG_NONE ? 0.f : g_y;
+        if (j == 0) GmU = S4<float>{0.f, 0.f, poutP - q0.r * g * S.dy, 0.f};
+        if (j == Ny - 1) GpU = S4<float>{0.f, 0.f, poutM + q0.r * g * S.dy, 0.f};
+      }
+    }
 
     // update in the reference's order: x flux, x gravity, y flux, y gravity,
     // conduction, viscosity (Update.h:114-168, 176-191)
@@ -177,34 +254,49 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
     un[2] += (Fw.v - Fe.v) * dtdx;
     un[3] += (Fw.p - Fe.p) * dtdx;
     if (S.grav) {
-      un[2] += S.dt * q0.r * S.gx;
-      un[3] += S.dt * 0.5f * (Fw.r + Fe.r) * S.gx;
+      un[2] += S.dt * q0.r * g_x;
+      un[3] += S.dt * 0.5f * (Fw.r + Fe.r) * g_x;
     }
-    un[0] += (Gm.r - Gp.r) * dtdy;
-    un[1] += (Gm.u - Gp.u) * dtdy;
-    un[2] += (Gm.v - Gp.v) * dtdy;
-    un[3] += (Gm.p - Gp.p) * dtdy;
+    un[0] += (GmU.r - GpU.r) * dtdy;
+    un[1] += (GmU.u - GpU.u) * dtdy;
+    un[2] += (GmU.v - GpU.v) * dtdy;
+    un[3] += (GmU.p - GpU.p) * dtdy;
     if (S.grav) {
-      un[2] += S.dt * q0.r * S.gy;
-      un[3] += S.dt * 0.5f * (Gm.r + Gp.r) * S.gy;
+      un[2] += S.dt * q0.r * g_y;
+      un[3] += S.dt * 0.5f * (GmU.r + GpU.r) * g_y;
     }
     if (S.tc) {
       const float TC = q0.p / q0.r;
       const float TL = __shfl_up_sync(0xffffffffu, TC, 1), TR = __shfl_down_sync(0xffffffffu, TC, 1);
       const float TU = qm.p / qm.r, TD = qp.p / qp.r;
-      const float FL = S.kappa * (TC - TL) * S.inv_dx, FR = S.kappa * (TR - TC) * S.inv_dx;
-      const float FU = S.kappa * (TC - TU) * S.inv_dy, FD = S.kappa * (TD - TC) * S.inv_dy;
+      float kL = S.kappa, kR = S.kappa, kU = S.kappa, kD = S.kappa;
+      if constexpr (EXT) {
+        if (S.tc == BK_ROW) {
+          const float *rw = S.rows + j * kRowStride;
+          kL = rw[ROW_KL]; kR = rw[ROW_KR]; kU = rw[ROW_KU]; kD = rw[ROW_KD];
+        }
+      }
+      float FL = kL * (TC - TL) * S.inv_dx, FR = kR * (TR - TC) * S.inv_dx;
+      const float FU = kU * (TC - TU) * S.inv_dy, FD = kD * (TD - TC) * S.inv_dy;
+      if constexpr (EXT) {
+        // the y-boundary modes replace the x-face fluxes FL / FR
+        // (ThermalConduction.h:75-103, as the reference writes them)
+        if (j == 0 && S.bctc_lo == FV2D_BCTC_FIXED_TEMPERATURE) FL = kL * 2.f * (TC - S.bctc_lo_v) * S.inv_dy;
+        if (j == 0 && S.bctc_lo == FV2D_BCTC_FIXED_GRADIENT) FL = kL * S.bctc_lo_v;
+        if (j == Ny - 1 && S.bctc_hi == FV2D_BCTC_FIXED_TEMPERATURE) FR = kR * 2.f * (S.bctc_hi_v - TC) * S.inv_dy;
+        if (j == Ny - 1 && S.bctc_hi == FV2D_BCTC_FIXED_GRADIENT) FR = kR * S.bctc_hi_v;
+      }
       un[3] += dtdx * (FR - FL) + dtdy * (FD - FU);
     }
     if (S.visc) {
       // 3x3 stencil of velocities: rows C-1, C, C+1 (qm, q0, qp) x lanes -1, 0, +1
       const float odx = S.inv_dx, ody = S.inv_dy, mu = S.mu;
       float u_[3][3], v_[3][3];
-      const S4<float> *rows[3] = {&qm, &q0, &qp};
+      const S4<float> *rws[3] = {&qm, &q0, &qp};
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
-        u_[r][1] = rows[r]->u;
-        v_[r][1] = rows[r]->v;
+        u_[r][1] = rws[r]->u;
+        v_[r][1] = rws[r]->v;
         u_[r][0] = __shfl_up_sync(0xffffffffu, u_[r][1], 1);
         v_[r][0] = __shfl_up_sync(0xffffffffu, v_[r][1], 1);
         u_[r][2] = __shfl_down_sync(0xffffffffu, u_[r][1], 1);
@@ -244,29 +336,37 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
     }
 
     if (out_lane) {
-      const int i = gxl - 2, j = C - 2;
+      const int i = gxl - 2;
       const long long g = (long long)C * S.P + gxl;
+      if (S.avg) {  // SSP-RK2: 0.5 (U^n + U**) (Update.h:214-220), offsets alike
+#pragma unroll
+        for (int k = 0; k < 4; ++k) un[k] = 0.5f * (S.dst[k * S.PL + g] + un[k]);
+      }
 #pragma unroll
       for (int k = 0; k < 4; ++k) S.dst[k * S.PL + g] = un[k];
-      // primitive state of the new cell for the next dt
-      float r = un[0], u = un[1] / r, v = un[2] / r;
-      float p = pressure_of(un[3], r, u, v, S.gm1, S.lowmach);
-      nnan += is_nan_f(r) | is_nan_f(u) | is_nan_f(v) | is_nan_f(p);
-      nneg += (r < 0.f) + (p < 0.f);
-      if (r < 0.f) r = 1e-8f;
-      if (p < 0.f) p = 1e-8f;
-      const float cs = sqrtf(p * S.gamma / r);
-      const float ih = (cs + fabsf(u)) * S.inv_dx + (cs + fabsf(v)) * S.inv_dy;
-      if (ih > lmax) lmax = ih;  // NaN never enters
+      if (S.last) {
+        // primitive state of the new cell for the next dt, negative guard
+        float r = un[0] + S.bg_r, u = un[1] / r, v = un[2] / r;
+        float p = pressure_of(un[3], S.bg_e, r, u, v, S.gm1, S.lowmach);
+        nnan += is_nan_f(r) | is_nan_f(u) | is_nan_f(v) | is_nan_f(p);
+        nneg += (r < 0.f) + (p < 0.f);
+        if (r < 0.f) r = 1e-8f;
+        if (p < 0.f) p = 1e-8f;
+        const float cs = sqrtf(p * S.gamma / r);
+        const float ih = (cs + fabsf(u)) * S.inv_dx + (cs + fabsf(v)) * S.inv_dy;
+        if (ih > lmax) lmax = ih;  // NaN never enters
+      } else {
+        nnan += is_nan_f(un[0]) | is_nan_f(un[1]) | is_nan_f(un[2]) | is_nan_f(un[3]);
+      }
       // ghost copies (BoundaryConditions.h:82-147, inverse map)
-      const bool ex = (i < 2 || i >= N - 2), ey = (j < 2 || j >= N - 2);
+      const bool ex = (i < 2 || i >= Nx - 2), ey = (j < 2 || j >= Ny - 2);
       if (ex || ey) {
         int tx[5], ty[5];
         bool nx[5], ny[5];
         tx[0] = i; nx[0] = false;
         ty[0] = j; ny[0] = false;
-        const int cx = 1 + (ex ? ghost_targets(i, N, S.bcx, tx + 1, nx + 1) : 0);
-        const int cy = 1 + (ey ? ghost_targets(j, N, S.bcy, ty + 1, ny + 1) : 0);
+        const int cx = 1 + (ex ? ghost_targets(i, Nx, S.bcx, tx + 1, nx + 1) : 0);
+        const int cy = 1 + (ey ? ghost_targets(j, Ny, S.bcy, ty + 1, ny + 1) : 0);
         for (int b = 0; b < cy; ++b)
           for (int c = 0; c < cx; ++c) {
             if (b == 0 && c == 0) continue;
@@ -284,7 +384,10 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
     q0 = qp;
     qp = qn;
     h0 = hp;
+    if constexpr (MH) hx0 = hxp;
+    qt0 = qtp;
     Gm = Gp;
+    poutM = poutP;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       U0[k] = Up[k];
@@ -299,43 +402,18 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
   const unsigned wnan = __reduce_add_sync(0xffffffffu, nnan);
   if (lane == 0) {
     SimDev *Gw = a.sims + item.sim;
-    atomicMax(&Gw->acc_bits, __float_as_uint(lmax));
+    if (S.last) atomicMax(&Gw->acc_bits, __float_as_uint(lmax));
     if (wn) atomicAdd(&Gw->negatives, (unsigned long long)wn);
     if (wnan) atomicAdd(&Gw->nan_cells, wnan);
     __threadfence();
     const unsigned t = atomicAdd(&Gw->ticket, 1u);
-    if (t == (unsigned)(G->ntx * G->nty) - 1u) {
-      // commit this simulation's step (ComputeDt.h:64, main.cpp:62, 83)
-      __threadfence();
-      volatile SimDev *V = Gw;
-      const double ih = (double)__uint_as_float(atomicAdd(&Gw->acc_bits, 0u));
-      double m = ih;
-      if (m < V->inv_tc) m = V->inv_tc;
-      if (m < V->inv_visc) m = V->inv_visc;
-      const double dtn = V->cfl / m;
-      const double t_new = V->t + V->dt;
-      const int step = V->step + 1;
-      V->t = t_new;
-      V->step = step;
-      V->cur = 1 - S.cur;
-      V->dt = dtn;
-      V->acc_bits = 0u;
-      int status = SIM_ACTIVE;
-      if (!(dtn > 0.0) || isinf(dtn) || V->nan_cells)  // the NaN / dt guard fails this request only
-        status = SIM_FAILED;
-      else if (step >= V->max_steps || !(t_new + V->eps < V->tend))
-        status = SIM_DONE;
-      V->status = status;
-      V->nan_cells = 0u;
-      __threadfence();
-      V->ticket = 0u;
-    }
+    if (t == (unsigned)(G->ntx * G->nty) - 1u) commit_stage(Gw);
   }
 }
 
+// The common family: HLL / HLLC x PCM / PLM.
 template <int H, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a) {
-  using namespace bm;
   const int lane = threadIdx.x & 31;
   const int nwarps = gridDim.x * (NT / 32);
   const int nw = *a.n_work;
@@ -344,18 +422,52 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a
     // volatile: the table changes between launches (commits, admissions)
     const volatile SimDev *G = a.sims + item.sim;
     if (G->status != SIM_ACTIVE) continue;
-    const bool plm = G->recon == 2;
+    const bool plm = G->recon == BR_PLM;
     if (G->rs == RS_HLL) {
       if (plm)
-        march_item<H, RS_HLL, true>(a, item, G, lane);
+        march_item<H, RS_HLL, BR_PLM, false>(a, item, G, lane);
       else
-        march_item<H, RS_HLL, false>(a, item, G, lane);
+        march_item<H, RS_HLL, BR_PCM, false>(a, item, G, lane);
     } else {
       if (plm)
-        march_item<H, RS_HLLC, true>(a, item, G, lane);
+        march_item<H, RS_HLLC, BR_PLM, false>(a, item, G, lane);
       else
-        march_item<H, RS_HLLC, false>(a, item, G, lane);
+        march_item<H, RS_HLLC, BR_PCM, false>(a, item, G, lane);
     }
+    __syncwarp();
+  }
+}
+
+template <int H, int RS>
+__device__ __forceinline__ void march_ext_recon(const BatchArgs &a, const WorkItem item, const volatile SimDev *G,
+                                                const int lane) {
+  const int recon = G->recon;
+  if (recon == BR_MH)
+    march_item<H, RS, BR_MH, true>(a, item, G, lane);
+  else if (recon == BR_PLM)
+    march_item<H, RS, BR_PLM, true>(a, item, G, lane);
+  else
+    march_item<H, RS, BR_PCM, true>(a, item, G, lane);
+}
+
+// The extended family: HLL / HLLC / FSLP x PCM / PLM / MUSCL-Hancock, with
+// the per-row tables and the boundary fluxes.
+template <int H, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) batch_march_ext_kernel(const BatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * (NT / 32);
+  const int nw = *a.n_work;
+  for (int w = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); w < nw; w += nwarps) {
+    const WorkItem item = a.work[w];
+    const volatile SimDev *G = a.sims + item.sim;
+    if (G->status != SIM_ACTIVE) continue;
+    const int rs = G->rs;
+    if (rs == RS_HLL)
+      march_ext_recon<H, RS_HLL>(a, item, G, lane);
+    else if (rs == RS_FSLP)
+      march_ext_recon<H, RS_FSLP>(a, item, G, lane);
+    else
+      march_ext_recon<H, RS_HLLC>(a, item, G, lane);
     __syncwarp();
   }
 }

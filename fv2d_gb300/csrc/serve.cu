@@ -41,7 +41,7 @@
 
 namespace fv2d {
 int batch_num_cfgs();
-void batch_cfg_info(int i, int *tx, int *ty, int *nt, int *staging, size_t *smem, const char **name);
+void batch_cfg_info(int i, int *tx, int *ty, int *nt, int *staging, size_t *smem, const char **name, int *ext);
 cudaError_t batch_setup(int i, int *ctas_per_sm);
 cudaError_t batch_launch(int i, int grid, cudaStream_t s, const BatchArgs &a);
 }  // namespace fv2d
@@ -51,25 +51,42 @@ using namespace fv2d;
 namespace {
 
 constexpr int kBuckets = 4;
+// Work lists, kernel launches and graph branches are per lane: a grid-size
+// bucket of one kernel family (lanes 0-3 the common family, 4-7 the extended
+// one).
+constexpr int kLanes = 2 * kBuckets;
 constexpr int kMaxCfgs = 32;  // capacity of the per-configuration tables (batch_kernels.cu asserts the bound)
 int num_cfgs() { return std::min(batch_num_cfgs(), kMaxCfgs); }
 constexpr int kConsBlocks = 64;
+constexpr int kMinSide = 16, kMaxSide = 8192;  // accepted Nx, Ny
 
-int bucket_of(int N) { return N < 128 ? 0 : (N < 256 ? 1 : (N < 512 ? 2 : 3)); }
+// Grid-size bucket of an Nx x Ny grid, by its cell count (the side of the
+// square with as many cells: < 128, < 256, < 512, larger).
+int bucket_of(int Nx, int Ny) {
+  const double c = (double)Nx * Ny;
+  return c < 128.0 * 128 ? 0 : (c < 256.0 * 256 ? 1 : (c < 512.0 * 512 ? 2 : 3));
+}
+int cfg_ext(int c) {
+  int e = 0;
+  batch_cfg_info(c, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &e);
+  return e;
+}
 
 // ---------------------------------------------------------------- kernels
 // Initial state of one simulation: every padded cell (ghosts included) takes
 // the binary64 initial condition of its source cell (BoundaryConditions.h
-// maps), converted to conservative variables and stored in binary32.
-__global__ void ic_kernel(fv2d_params p, int problem, float *U, long long plane, int pitch, int N) {
+// maps), converted to conservative variables and stored in binary32 as the
+// offset from the background (bg_r, 0, 0, bg_e).
+__global__ void ic_kernel(fv2d_params p, int problem, float *U, long long plane, int pitch, int Nx, int Ny,
+                          float bg_r, float bg_e) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int W = N + 4;
-  if (idx >= (long long)W * W) return;
+  const int W = Nx + 4;
+  if (idx >= (long long)W * (Ny + 4)) return;
   const int py = (int)(idx / W), px = (int)(idx % W);
   int sx = px - 2, sy = py - 2;
   bool nx = false, ny = false;
-  if (sx < 0 || sx >= N) sx = ghost_source(sx, N, p.boundary_x, &nx);
-  if (sy < 0 || sy >= N) sy = ghost_source(sy, N, p.boundary_y, &ny);
+  if (sx < 0 || sx >= Nx) sx = ghost_source(sx, Nx, p.boundary_x, &nx);
+  if (sy < 0 || sy >= Ny) sy = ghost_source(sy, Ny, p.boundary_y, &ny);
   double q[4];
   init_cell(p, problem, sx, sy, q);
   if (nx) q[1] = -q[1];
@@ -77,25 +94,53 @@ __global__ void ic_kernel(fv2d_params p, int problem, float *U, long long plane,
   const Gas<double> g{p.gamma0, p.gamma0 - 1.0, 1.0 / (p.gamma0 - 1.0), 0.0};
   const S4<double> u = prim_to_cons(S4<double>{q[0], q[1], q[2], q[3]}, g);
   const long long o = (long long)py * pitch + px;
-  U[o] = (float)u.r;
+  U[o] = (float)(u.r - (double)bg_r);
   U[plane + o] = (float)u.u;
   U[2 * plane + o] = (float)u.v;
-  U[3 * plane + o] = (float)u.p;
+  U[3 * plane + o] = (float)(u.p - (double)bg_e);
+}
+
+// Per-row table of simulation `slot`: the row's gravity (Gravity.h:15-37,
+// narrowed to float like :16, 39) and face conductivities
+// (ThermalConduction.h:9-26, 46-53: the neighbour conductivities are taken at
+// the physical coordinates converted to int, as the reference calls them).
+__device__ double row_kappa(const fv2d_params &p, int jj) {  // padded row jj
+  if (p.thermal_conductivity_mode == FV2D_TCM_B02) {
+    const double dy = (p.ymax - p.ymin) / p.Ny;
+    const double y = p.ymin + (jj - p.Nghosts + 0.5) * dy;
+    const double tr = (tanh((y - p.b02_ymid) / p.b02_thickness) + 1.0) * 0.5;
+    return p.kappa * (p.b02_kappa1 * (1.0 - tr) + p.b02_kappa2 * tr);
+  }
+  return p.kappa;
+}
+__global__ void rows_kernel(fv2d_params p, float *rows) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.Ny) return;
+  const double dy = (p.ymax - p.ymin) / p.Ny;
+  const double y = p.ymin + ((double)j + 0.5) * dy;
+  float *r = rows + (size_t)j * kRowStride;
+  r[ROW_G] = (float)(p.hot_bubble_g0 * sin(y * M_PI * 2.0 / p.ymax));
+  const double kC = row_kappa(p, j + p.Nghosts);
+  r[ROW_KL] = (float)(0.5 * (kC + row_kappa(p, (int)y)));
+  r[ROW_KR] = (float)(0.5 * (kC + row_kappa(p, (int)y)));
+  r[ROW_KU] = (float)(0.5 * (kC + row_kappa(p, (int)(y - dy))));
+  r[ROW_KD] = (float)(0.5 * (kC + row_kappa(p, (int)(y + dy))));
+  r[5] = r[6] = r[7] = 0.f;
 }
 
 // Inverse hyperbolic dt of the current state of simulation `slot` (same
 // per-cell expression as the step epilogue), max into acc_bits.
 __global__ void first_dt_kernel(SimDev *sims, int slot) {
   const SimDev &S = sims[slot];
-  const int N = S.N;
+  const int Nx = S.Nx;
   const float *U = S.U[S.cur];
   float m = 0.f;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < (long long)N * N;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < (long long)Nx * S.Ny;
        c += (long long)gridDim.x * blockDim.x) {
-    const int j = (int)(c / N), i = (int)(c % N);
+    const int j = (int)(c / Nx), i = (int)(c % Nx);
     const long long g = (long long)(j + 2) * S.pitch + (i + 2);
-    float r = U[g], u = U[S.plane + g] / r, v = U[2 * S.plane + g] / r;
-    float p = pressure_of(U[3 * S.plane + g], r, u, v, S.gm1, S.lowmach);
+    float r = U[g] + S.bg_r, u = U[S.plane + g] / r, v = U[2 * S.plane + g] / r;
+    float p = pressure_of(U[3 * S.plane + g], S.bg_e, r, u, v, S.gm1, S.lowmach);
     if (r < 0.f) r = 1e-8f;
     if (p < 0.f) p = 1e-8f;
     const float cs = sqrtf(p * S.gamma / r);
@@ -126,14 +171,15 @@ __device__ __forceinline__ void neumaier_add(double &s, double &c, double x) {
 }
 __global__ void __launch_bounds__(256) cons_kernel(const SimDev *sims, int slot, double *out) {
   const SimDev &S = sims[slot];
-  const int N = S.N;
+  const int Nx = S.Nx;
   const float *U = S.U[S.cur];
+  const double bg[4] = {(double)S.bg_r, 0.0, 0.0, (double)S.bg_e};
   double s[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < (long long)N * N;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < (long long)Nx * S.Ny;
        k += (long long)gridDim.x * blockDim.x) {
-    const int j = (int)(k / N), i = (int)(k % N);
+    const int j = (int)(k / Nx), i = (int)(k % Nx);
     const long long g = (long long)(j + 2) * S.pitch + (i + 2);
-    for (int f = 0; f < 4; ++f) neumaier_add(s[f], c[f], (double)U[f * S.plane + g]);
+    for (int f = 0; f < 4; ++f) neumaier_add(s[f], c[f], (double)U[f * S.plane + g] + bg[f]);
   }
   // pairwise tree over the block, carrying the compensation terms
   __shared__ double sh[8][256];
@@ -179,7 +225,7 @@ struct Slot {
   bool used = false;
   int64_t id = -1;
   fv2d_request req;
-  int bucket = 0, cfg = 0;
+  int bucket = 0, lane = 0, cfg = 0;
   void *mem = nullptr;
   size_t bytes = 0;
   double submit_s = 0, admit_s = 0;
@@ -190,8 +236,9 @@ struct Slot {
 
 struct Finished {
   fv2d_result res;
-  std::vector<float> U;  // interior conservative planes, N x N each
+  std::vector<float> U;  // interior conservative offset planes, Ny x Nx each
   double gamma;
+  double bg_r, bg_e;     // background of the offsets
 };
 
 }  // namespace
@@ -208,18 +255,22 @@ struct fv2d_server {
   CUtensorMap *d_tmaps = nullptr, *h_tmaps = nullptr;
   std::vector<Slot> slots;
   std::vector<int> free_slots;
-  // per-bucket work lists
-  WorkItem *d_work[kBuckets] = {};
+  // per-lane work lists (lane = bucket, + kBuckets for the extended family)
+  WorkItem *d_work[kLanes] = {};
   int *d_nwork = nullptr, *h_nwork = nullptr;
-  WorkItem *h_work[kBuckets] = {};
-  int work_cap[kBuckets] = {};
-  int items_in[kBuckets] = {};  // work items of the resident requests, per bucket
-  int bucket_cfg[kBuckets] = {1, 2, 3, 3};
+  WorkItem *h_work[kLanes] = {};
+  int work_cap[kLanes] = {};
+  int items_in[kLanes] = {};  // work items of the resident requests, per lane
+  int bucket_cfg[kBuckets] = {1, 2, 3, 3};  // common-family configuration per bucket
+  int ext_cfg = -1;                         // extended-family configuration (every bucket)
   int cfg_grid[kMaxCfgs] = {};
   bool lists_dirty = true;
   int mask = 0;
-  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (K, bucket mask) -> graph
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (K, lane mask) -> graph
   double *d_cons = nullptr, *h_cons = nullptr;
+  // kernel control words (BatchArgs::ctl): fault bits, tile-copy wait limit
+  unsigned int *d_ctl = nullptr, *h_ctl = nullptr;
+  std::atomic<uint32_t> wait_limit_req{0};  // test hook: a new wait limit for the worker to apply (0: none)
   float *h_stage = nullptr;
   size_t h_stage_size = 0;
   Arena<DeviceMemory> arena;
@@ -244,10 +295,10 @@ struct fv2d_server {
   } pub;
   double rate_est = 2e10;  // cell-updates/s, refined by measurement
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // the buckets' step chains run as parallel branches of a replay graph
-  cudaStream_t bstream[kBuckets] = {};
-  cudaEvent_t ev_fork = nullptr, ev_join[kBuckets] = {};
-  double sched_cells = 0;  // cells advanced per step by the current work lists
+  // the lanes' step chains run as parallel branches of a replay graph
+  cudaStream_t bstream[kLanes] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {};
+  double sched_cells = 0;  // cell-stages advanced per launch by the current work lists
   // failure state: `fault` is written by the worker alone; `broken`,
   // `fail_code` and `err` are set once, under mu, when the worker stops
   std::string fault;
@@ -278,19 +329,50 @@ const char *check_request(const fv2d_request &r) {
   const fv2d_params &p = r.params;
   if (r.struct_size != sizeof(fv2d_request)) return "fv2d_request.struct_size mismatch";
   if (const char *w = validate(p)) return w;
-  if (p.Nx != p.Ny) return "the service runs square grids (Nx == Ny)";
-  if (p.Nx % 32 != 0 || p.Nx < 64 || p.Nx > 4096) return "N must be a multiple of 32 in [64, 4096]";
+  if (p.Nx < kMinSide || p.Nx > kMaxSide || p.Ny < kMinSide || p.Ny > kMaxSide)
+    return "Nx and Ny must be in [16, 8192]";
   if (!problem_valid(r.problem)) return "unknown problem";
-  if (p.reconstruction != FV2D_PCM && p.reconstruction != FV2D_PCM_WB && p.reconstruction != FV2D_PLM)
-    return "the service provides PCM and PLM reconstruction";
-  if (p.riemann_solver == FV2D_FSLP) return "the service provides HLL and HLLC";
-  if (p.time_stepping != FV2D_TS_EULER) return "the service provides Euler stepping";
-  if (p.gravity_mode == FV2D_GRAV_ANALYTICAL || p.well_balanced_flux_at_y_bc) return "constant gravity only";
-  if (p.thermal_conductivity_active && (p.thermal_conductivity_mode != FV2D_TCM_CONSTANT ||
-                                        p.bctc_ymin != FV2D_BCTC_NONE || p.bctc_ymax != FV2D_BCTC_NONE))
-    return "constant conductivity without boundary modes only";
   if (r.max_steps < 0) return "max_steps < 0";
   return nullptr;
+}
+
+// The kernel family a request needs: the extended one for FSLP, the
+// MUSCL-Hancock predictor, analytical gravity, B02 conductivity, the
+// y-boundary conduction modes and the well-balanced y flux.
+bool needs_ext(const fv2d_params &p) {
+  return p.riemann_solver == FV2D_FSLP || p.reconstruction == FV2D_MUSCL_HANCOCK ||
+         p.gravity_mode == FV2D_GRAV_ANALYTICAL || p.well_balanced_flux_at_y_bc ||
+         (p.thermal_conductivity_active && (p.thermal_conductivity_mode != FV2D_TCM_CONSTANT ||
+                                            p.bctc_ymin != FV2D_BCTC_NONE || p.bctc_ymax != FV2D_BCTC_NONE));
+}
+bool needs_rows(const fv2d_params &p) {
+  return p.gravity_mode == FV2D_GRAV_ANALYTICAL ||
+         (p.thermal_conductivity_active && p.thermal_conductivity_mode != FV2D_TCM_CONSTANT);
+}
+
+// Background of the stored offsets: the median density and total energy of
+// the initial condition, sampled on at most 64 x 64 cells (momenta have none:
+// reflections negate them).
+void background(const fv2d_request &r, float *bg_r, float *bg_e) {
+  const fv2d_params &p = r.params;
+  const int sx = std::max(1, p.Nx / 64), sy = std::max(1, p.Ny / 64);
+  std::vector<double> rs, es;
+  const Gas<double> g{p.gamma0, p.gamma0 - 1.0, 1.0 / (p.gamma0 - 1.0), 0.0};
+  for (int j = sy / 2; j < p.Ny; j += sy)
+    for (int i = sx / 2; i < p.Nx; i += sx) {
+      double q[4];
+      init_cell(p, r.problem, i, j, q);
+      const S4<double> u = prim_to_cons(S4<double>{q[0], q[1], q[2], q[3]}, g);
+      rs.push_back(u.r);
+      es.push_back(u.p);
+    }
+  auto median = [](std::vector<double> &v) {
+    std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+    return v[v.size() / 2];
+  };
+  const double mr = median(rs), me = median(es);
+  *bg_r = std::isfinite(mr) ? (float)mr : 0.f;
+  *bg_e = std::isfinite(me) ? (float)me : 0.f;
 }
 
 // Synchronises the worker's stream.  A failure is recorded in s->fault: the
@@ -302,13 +384,19 @@ bool sync_stream(fv2d_server *s) {
   return false;
 }
 
-size_t state_bytes(int N, int *pitch, long long *plane) {
-  *pitch = (N + 4 + 31) / 32 * 32;
-  *plane = (long long)(N + 4) * *pitch;
-  return sizeof(float) * 8 * (size_t)*plane;  // two buffers x four planes
+// Device bytes of a simulation: two buffers of four planes with the ghost
+// ring, then (when the request needs it) its per-row table.
+size_t state_bytes(const fv2d_params &p, int *pitch, long long *plane, size_t *rows_off) {
+  *pitch = (p.Nx + 4 + 31) / 32 * 32;
+  *plane = (long long)(p.Ny + 4) * *pitch;
+  const size_t planes = sizeof(float) * 8 * (size_t)*plane;  // two buffers x four planes
+  *rows_off = (planes + 255) & ~size_t(255);
+  return needs_rows(p) ? *rows_off + sizeof(float) * kRowStride * (size_t)p.Ny : planes;
 }
 
-// Grow bucket b's work-list buffers to hold `need` items.  New buffers are
+int lane_cfg(const fv2d_server *s, int lane) { return lane < kBuckets ? s->bucket_cfg[lane] : s->ext_cfg; }
+
+// Grow lane b's work-list buffers to hold `need` items.  New buffers are
 // allocated before the old ones are released, so a failure leaves the lists
 // as they were.
 bool reserve_work(fv2d_server *s, int b, int need) {
@@ -341,23 +429,29 @@ int admit(fv2d_server *s, const Pending &pd) {
   if (s->free_slots.empty()) return -1;
   const fv2d_request &r = pd.req;
   const fv2d_params &p = r.params;
-  const int N = p.Nx;
+  const int Nx = p.Nx, Ny = p.Ny;
   int pitch;
   long long plane;
-  const size_t bytes = state_bytes(N, &pitch, &plane);
-  const int bucket = bucket_of(N);
+  size_t rows_off;
+  const size_t bytes = state_bytes(p, &pitch, &plane, &rows_off);
+  const int bucket = bucket_of(Nx, Ny);
+  const bool ext = needs_ext(p);
+  const int lane = bucket + (ext ? kBuckets : 0);
+  const int cfg = lane_cfg(s, lane);
   int tx, ty, nt, staging;
-  batch_cfg_info(s->bucket_cfg[bucket], &tx, &ty, &nt, &staging, nullptr, nullptr);
-  const int items = ((N + tx - 1) / tx) * ((N + ty - 1) / ty);
+  batch_cfg_info(cfg, &tx, &ty, &nt, &staging, nullptr, nullptr, nullptr);
+  const int items = ((Nx + tx - 1) / tx) * ((Ny + ty - 1) / ty);
+  float bg_r = 0.f, bg_e = 0.f;
+  background(r, &bg_r, &bg_e);
   // state memory first: a request that does not fit must not grow the work
   // lists (that synchronises the stream and drops the captured graphs)
   void *mem = s->arena.alloc(bytes);
   if (!mem) return -1;
-  if (!reserve_work(s, bucket, s->items_in[bucket] + items)) {
+  if (!reserve_work(s, lane, s->items_in[lane] + items)) {
     s->arena.release(mem, bytes);
     return -1;
   }
-  s->items_in[bucket] += items;
+  s->items_in[lane] += items;
   const int slot = s->free_slots.back();
   s->free_slots.pop_back();
   Slot &sl = s->slots[slot];
@@ -365,7 +459,8 @@ int admit(fv2d_server *s, const Pending &pd) {
   sl.id = pd.id;
   sl.req = r;
   sl.bucket = bucket;
-  sl.cfg = s->bucket_cfg[bucket];
+  sl.lane = lane;
+  sl.cfg = cfg;
   sl.mem = mem;
   sl.bytes = bytes;
   sl.submit_s = pd.submit_s;
@@ -377,15 +472,19 @@ int admit(fv2d_server *s, const Pending &pd) {
   std::memset(&d, 0, sizeof(d));
   d.U[0] = static_cast<float *>(mem);
   d.U[1] = static_cast<float *>(mem) + 4 * plane;
+  d.rows = needs_rows(p) ? reinterpret_cast<const float *>(static_cast<char *>(mem) + rows_off) : nullptr;
   d.plane = plane;
   d.pitch = pitch;
-  d.N = N;
-  d.ntx = (N + tx - 1) / tx;
-  d.nty = (N + ty - 1) / ty;
+  d.Nx = Nx;
+  d.Ny = Ny;
+  d.ntx = (Nx + tx - 1) / tx;
+  d.nty = (Ny + ty - 1) / ty;
   d.cur = 0;
   d.status = SIM_ACTIVE;
   d.step = 0;
   d.max_steps = r.max_steps;
+  d.ts = p.time_stepping == FV2D_TS_RK2 ? 1 : 0;
+  d.stage = 0;
   d.t = 0.0;
   d.dt = 0.0;
   d.tend = r.tend > 0 ? r.tend : INFINITY;
@@ -395,29 +494,41 @@ int admit(fv2d_server *s, const Pending &pd) {
   d.gamma = (float)p.gamma0;
   d.gm1 = (float)(p.gamma0 - 1.0);
   d.entho = (float)(1.0 / (p.gamma0 - 1.0));
-  const double dx = (p.xmax - p.xmin) / N, dy = (p.ymax - p.ymin) / N;
+  d.fslp_K = (float)p.fslp_K;
+  const double dx = (p.xmax - p.xmin) / Nx, dy = (p.ymax - p.ymin) / Ny;
   d.dx = (float)dx;
   d.dy = (float)dy;
   d.inv_dx = (float)(1.0 / dx);
   d.inv_dy = (float)(1.0 / dy);
   d.gx = (float)p.gx;
   d.gy = (float)p.gy;
+  d.gdx = (float)(p.gx * dx);
+  d.gdy = (float)(p.gy * dy);
   d.kappa = (float)p.kappa;
   d.mu = (float)p.mu;
-  d.rs = p.riemann_solver == FV2D_HLL ? RS_HLL : RS_HLLC;
-  d.recon = p.reconstruction == FV2D_PLM ? 2 : 0;
+  d.bg_r = bg_r;
+  d.bg_e = bg_e;
+  d.rs = p.riemann_solver == FV2D_HLL ? RS_HLL : (p.riemann_solver == FV2D_FSLP ? RS_FSLP : RS_HLLC);
+  d.recon = p.reconstruction == FV2D_PLM ? BR_PLM : (p.reconstruction == FV2D_MUSCL_HANCOCK ? BR_MH : BR_PCM);
+  d.ext = ext ? 1 : 0;
   d.bcx = p.boundary_x;
   d.bcy = p.boundary_y;
-  d.grav = p.gravity_mode == FV2D_GRAV_CONSTANT;
-  d.tc = p.thermal_conductivity_active ? 1 : 0;
+  d.grav = p.gravity_mode == FV2D_GRAV_CONSTANT ? BG_CONST : (p.gravity_mode == FV2D_GRAV_ANALYTICAL ? BG_ROW : BG_NONE);
+  d.tc = !p.thermal_conductivity_active ? BK_NONE
+                                        : (p.thermal_conductivity_mode == FV2D_TCM_CONSTANT ? BK_CONST : BK_ROW);
   d.visc = p.viscosity_active ? 1 : 0;
+  d.wb = p.well_balanced_flux_at_y_bc ? 1 : 0;
+  d.bctc_lo = p.thermal_conductivity_active ? p.bctc_ymin : FV2D_BCTC_NONE;
+  d.bctc_hi = p.thermal_conductivity_active ? p.bctc_ymax : FV2D_BCTC_NONE;
+  d.bctc_lo_v = (float)p.bctc_ymin_value;
+  d.bctc_hi_v = (float)p.bctc_ymax_value;
   d.lowmach = r.lowmach ? 1 : 0;
   d.tma_ok = 0;
   if (staging == 1) {  // TMA staging needs the tensor maps
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     bool ok = enc != nullptr;
     for (int b = 0; b < 2 && ok; ++b) {
-      cuuint64_t dims[3] = {(cuuint64_t)(N + 4), (cuuint64_t)(N + 4), 4};
+      cuuint64_t dims[3] = {(cuuint64_t)(Nx + 4), (cuuint64_t)(Ny + 4), 4};
       cuuint64_t strides[2] = {(cuuint64_t)pitch * 4, (cuuint64_t)plane * 4};
       cuuint32_t box[3] = {(cuuint32_t)(tx + 4), (cuuint32_t)(ty + 4), 4};
       cuuint32_t es[3] = {1, 1, 1};
@@ -431,9 +542,12 @@ int admit(fv2d_server *s, const Pending &pd) {
                       s->stream);
   }
   cudaMemcpyAsync(&s->d_sims[slot], &d, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream);
-  const long long W = N + 4;
-  ic_kernel<<<(unsigned)((W * W + 255) / 256), 256, 0, s->stream>>>(p, r.problem, d.U[0], plane, pitch, N);
-  const int nb = (int)std::min<long long>(1024, ((long long)N * N + 255) / 256);
+  const long long cells_padded = (long long)(Nx + 4) * (Ny + 4);
+  ic_kernel<<<(unsigned)((cells_padded + 255) / 256), 256, 0, s->stream>>>(p, r.problem, d.U[0], plane, pitch, Nx,
+                                                                              Ny, bg_r, bg_e);
+  if (d.rows)
+    rows_kernel<<<(Ny + 127) / 128, 128, 0, s->stream>>>(p, const_cast<float *>(d.rows));
+  const int nb = (int)std::min<long long>(1024, ((long long)Nx * Ny + 255) / 256);
   first_dt_kernel<<<nb, 256, 0, s->stream>>>(s->d_sims, slot);
   first_dt_finish<<<1, 1, 0, s->stream>>>(s->d_sims, slot);
   if (pd.id > 0)  // the autotuner's synthetic states need no sums
@@ -485,12 +599,15 @@ void publish_locked(fv2d_server *s) {
   s->pub.bytes_reserved = (double)s->arena.reserved;
 }
 
+// Launches a step of this request takes (SSP-RK2: two stages).
+int stages_of(const fv2d_params &p) { return p.time_stepping == FV2D_TS_RK2 ? 2 : 1; }
+
 // Remaining cell-updates of a resident request: its remaining steps (the
 // step limit, or the time limit at the last dt when that comes first) times
-// its cells.
+// its cells and stages.
 double remaining_work(const fv2d_server *s, int slot) {
   const Slot &sl = s->slots[slot];
-  const double cells = (double)sl.req.params.Nx * sl.req.params.Ny;
+  const double cells = (double)sl.req.params.Nx * sl.req.params.Ny * stages_of(sl.req.params);
   double steps = (double)sl.req.max_steps - sl.steps_seen;
   if (sl.steps_seen > 0 && sl.req.tend > 0) {
     const SimDev &d = s->h_down[slot];
@@ -500,26 +617,28 @@ double remaining_work(const fv2d_server *s, int slot) {
 }
 
 void rebuild_lists(fv2d_server *s) {
-  std::vector<WorkItem> lists[kBuckets];
+  std::vector<WorkItem> lists[kLanes];
   // shortest remaining work first, up to about active_cells cells per step
   // (every resident request when active_cells is 0)
   std::vector<Candidate> cand;
   for (int k = 0; k < s->max_sims; ++k)
-    if (s->slots[k].used)
+    if (s->slots[k].used) {
+      const fv2d_params &p = s->slots[k].req.params;
       cand.push_back({k, s->cfg.active_cells > 0 ? remaining_work(s, k) : 0.0,
-                      (double)s->slots[k].req.params.Nx * s->slots[k].req.params.Ny});
+                      (double)p.Nx * p.Ny * stages_of(p)});
+    }
   const std::vector<int> run = select_active(std::move(cand), s->cfg.active_cells);
-  // interleave tiles of the simulations of a bucket so that a CTA's
+  // interleave work items of the simulations of a lane so that a CTA's
   // consecutive items belong to different simulations
-  std::vector<int> per_bucket[kBuckets];
+  std::vector<int> per_lane[kLanes];
   s->sched_cells = 0;
   for (int k : run) {
-    per_bucket[s->slots[k].bucket].push_back(k);
+    per_lane[s->slots[k].lane].push_back(k);
     s->sched_cells += (double)s->slots[k].req.params.Nx * s->slots[k].req.params.Ny;
   }
   s->mask = 0;
-  for (int b = 0; b < kBuckets; ++b) {
-    for (int slot : per_bucket[b]) {
+  for (int b = 0; b < kLanes; ++b) {
+    for (int slot : per_lane[b]) {
       const SimDev &d = s->h_up[slot];
       for (int ty = 0; ty < d.nty; ++ty)
         for (int tx = 0; tx < d.ntx; ++tx) lists[b].push_back(WorkItem{slot, (short)tx, (short)ty});
@@ -533,15 +652,15 @@ void rebuild_lists(fv2d_server *s) {
       cudaMemcpyAsync(s->d_work[b], s->h_work[b], sizeof(WorkItem) * n, cudaMemcpyHostToDevice, s->stream);
     }
   }
-  cudaMemcpyAsync(s->d_nwork, s->h_nwork, sizeof(int) * kBuckets, cudaMemcpyHostToDevice, s->stream);
+  cudaMemcpyAsync(s->d_nwork, s->h_nwork, sizeof(int) * kLanes, cudaMemcpyHostToDevice, s->stream);
   s->lists_dirty = false;
 }
 
 cudaError_t launch_step(fv2d_server *s, int mask) {
-  for (int b = 0; b < kBuckets; ++b) {
+  for (int b = 0; b < kLanes; ++b) {
     if (!(mask & (1 << b))) continue;
-    BatchArgs a{s->d_sims, s->d_work[b], s->d_nwork + b, s->d_tmaps};
-    const int c = s->bucket_cfg[b];
+    BatchArgs a{s->d_sims, s->d_work[b], s->d_nwork + b, s->d_tmaps, s->d_ctl};
+    const int c = lane_cfg(s, b);
     cudaError_t e = batch_launch(c, s->cfg_grid[c], s->stream, a);
     if (e != cudaSuccess) return e;
   }
@@ -554,15 +673,15 @@ cudaGraphExec_t get_graph(fv2d_server *s, int K, int mask) {
   if (it != s->graphs.end()) return it->second;
   cudaGraph_t g;
   if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
-  // one branch per bucket: a request's steps depend only on its own previous
-  // step, so the buckets' chains are independent and a small bucket's
+  // one branch per lane: a request's steps depend only on its own previous
+  // step, so the lanes' chains are independent and a small bucket's
   // kernels can fill the SMs that a large one's leave idle
   cudaEventRecord(s->ev_fork, s->stream);
-  for (int b = 0; b < kBuckets; ++b) {
+  for (int b = 0; b < kLanes; ++b) {
     if (!(mask & (1 << b))) continue;
     cudaStreamWaitEvent(s->bstream[b], s->ev_fork, 0);
-    BatchArgs a{s->d_sims, s->d_work[b], s->d_nwork + b, s->d_tmaps};
-    const int c = s->bucket_cfg[b];
+    BatchArgs a{s->d_sims, s->d_work[b], s->d_nwork + b, s->d_tmaps, s->d_ctl};
+    const int c = lane_cfg(s, b);
     for (int k = 0; k < K; ++k) batch_launch(c, s->cfg_grid[c], s->bstream[b], a);
     cudaEventRecord(s->ev_join[b], s->bstream[b]);
     cudaStreamWaitEvent(s->stream, s->ev_join[b], 0);
@@ -584,8 +703,7 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
   std::vector<size_t> off(done.size());
   for (size_t k = 0; k < done.size(); ++k) {
     off[k] = need;
-    const int N = s->h_down[done[k]].N;
-    need += 4 * (size_t)N * N;
+    need += 4 * (size_t)s->h_down[done[k]].Nx * s->h_down[done[k]].Ny;
   }
   if (s->h_stage_size < need * sizeof(float)) {
     if (s->h_stage) cudaFreeHost(s->h_stage);
@@ -611,13 +729,13 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
   for (size_t k = 0; k < done.size(); ++k) {
     const int slot = done[k];
     const SimDev &d = s->h_down[slot];
-    const int N = d.N;
+    const int Nx = d.Nx, Ny = d.Ny;
     cons_kernel<<<kConsBlocks, 256, 0, s->stream>>>(s->d_sims, slot, s->d_cons + (size_t)slot * kConsBlocks * 8);
     cudaMemcpyAsync(s->h_cons + (size_t)slot * kConsBlocks * 8, s->d_cons + (size_t)slot * kConsBlocks * 8,
                     sizeof(double) * kConsBlocks * 8, cudaMemcpyDeviceToHost, s->stream);
     for (int f = 0; f < 4 && stage; ++f)
-      cudaMemcpy2DAsync(stage + off[k] + (size_t)f * N * N, sizeof(float) * N,
-                        d.U[d.cur] + f * d.plane + 2 * d.pitch + 2, sizeof(float) * d.pitch, sizeof(float) * N, N,
+      cudaMemcpy2DAsync(stage + off[k] + (size_t)f * Nx * Ny, sizeof(float) * Nx,
+                        d.U[d.cur] + f * d.plane + 2 * d.pitch + 2, sizeof(float) * d.pitch, sizeof(float) * Nx, Ny,
                         cudaMemcpyDeviceToHost, s->stream);
     // mark the device slot free so stale work-list entries are skipped
     s->h_up[slot].status = SIM_FREE;
@@ -630,19 +748,21 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
     const int slot = done[k];
     const SimDev &d = s->h_down[slot];
     Slot &sl = s->slots[slot];
-    const int N = d.N;
+    const size_t cells = (size_t)d.Nx * d.Ny;
     Finished fin;
     fv2d_result &r = fin.res;
     std::memset(&r, 0, sizeof(r));
     r.id = sl.id;
-    r.status = d.status == SIM_DONE ? FV2D_OK : FV2D_ERR_NUMERIC;
+    r.status = d.status == SIM_DONE ? FV2D_OK : (d.dev_err ? FV2D_ERR_CUDA : FV2D_ERR_NUMERIC);
     r.steps = d.step;
     r.t = d.t;
     r.submit_s = sl.submit_s;
     r.admit_s = sl.admit_s;
     r.negatives = d.negatives;
-    r.N = N;
+    r.Nx = d.Nx;
+    r.Ny = d.Ny;
     r.bucket = sl.bucket;
+    r.lane = sl.lane;
     const fv2d_params &p = sl.req.params;
     const double area = ((p.xmax - p.xmin) / p.Nx) * ((p.ymax - p.ymin) / p.Ny);
     double c1[4];
@@ -654,16 +774,18 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
     bool kept = false;
     if (stage) {
       try {
-        fin.U.assign(stage + off[k], stage + off[k] + 4 * (size_t)N * N);
+        fin.U.assign(stage + off[k], stage + off[k] + 4 * cells);
         kept = true;
       } catch (const std::bad_alloc &) {
       }
     }
     if (!kept && r.status == FV2D_OK) r.status = FV2D_ERR_NOMEM;
     fin.gamma = p.gamma0;
+    fin.bg_r = d.bg_r;
+    fin.bg_e = d.bg_e;
     r.done_s = t_done;
     s->arena.release(sl.mem, sl.bytes);
-    s->items_in[sl.bucket] -= d.ntx * d.nty;
+    s->items_in[sl.lane] -= d.ntx * d.nty;
     s->n_active--;
     sl.used = false;
     sl.mem = nullptr;
@@ -714,7 +836,12 @@ bool run_once(fv2d_server *s, int K_fixed) {
   for (int k = 0; k < s->max_sims; ++k)
     if (s->slots[k].used) hi = k + 1;
   cudaMemcpyAsync(s->h_down, s->d_sims, sizeof(SimDev) * hi, cudaMemcpyDeviceToHost, s->stream);
+  cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(unsigned int), cudaMemcpyDeviceToHost, s->stream);
   if (!sync_stream(s)) return true;
+  if (s->h_ctl[0]) {  // a CTA stopped with a tile copy in flight: shared memory can no longer be trusted
+    s->fault = "device: a tile copy of the served step did not complete within its bounded waits";
+    return true;
+  }
   float ms = 0;
   cudaEventElapsedTime(&ms, s->ev0, s->ev1);
   s->replays++;
@@ -726,7 +853,7 @@ bool run_once(fv2d_server *s, int K_fixed) {
     if (!sl.used) continue;
     const SimDev &d = s->h_down[k];
     const int new_steps = d.step - sl.steps_seen;
-    cells += (double)d.N * d.N * new_steps;
+    cells += (double)d.Nx * d.Ny * new_steps;
     sl.steps_seen = d.step;
     if (d.status == SIM_DONE || d.status == SIM_FAILED) done.push_back(k);
   }
@@ -752,7 +879,7 @@ void fail_all(fv2d_server *s, int code, const std::vector<Pending> &extra) noexc
     s->err = s->fault.empty() ? std::string("service stopped") : s->fault;
   } catch (const std::bad_alloc &) {
   }
-  auto post = [&](int64_t id, double submit_s, double admit_s, int N, int steps) {
+  auto post = [&](int64_t id, double submit_s, double admit_s, const fv2d_params &p, int steps) {
     fv2d_result r;
     std::memset(&r, 0, sizeof(r));
     r.id = id;
@@ -761,8 +888,10 @@ void fail_all(fv2d_server *s, int code, const std::vector<Pending> &extra) noexc
     r.submit_s = submit_s;
     r.admit_s = admit_s;
     r.done_s = t;
-    r.N = N;
-    r.bucket = bucket_of(N);
+    r.Nx = p.Nx;
+    r.Ny = p.Ny;
+    r.bucket = bucket_of(p.Nx, p.Ny);
+    r.lane = r.bucket + (needs_ext(p) ? kBuckets : 0);
     s->n_failed++;
     try {
       s->done_unpolled.push_back(r);
@@ -771,11 +900,11 @@ void fail_all(fv2d_server *s, int code, const std::vector<Pending> &extra) noexc
   };
   for (Slot &sl : s->slots)
     if (sl.used) {
-      post(sl.id, sl.submit_s, sl.admit_s, sl.req.params.Nx, sl.steps_seen);
+      post(sl.id, sl.submit_s, sl.admit_s, sl.req.params, sl.steps_seen);
       sl.used = false;
     }
-  for (const Pending &pd : s->queue) post(pd.id, pd.submit_s, -1.0, pd.req.params.Nx, 0);
-  for (const Pending &pd : extra) post(pd.id, pd.submit_s, -1.0, pd.req.params.Nx, 0);
+  for (const Pending &pd : s->queue) post(pd.id, pd.submit_s, -1.0, pd.req.params, 0);
+  for (const Pending &pd : extra) post(pd.id, pd.submit_s, -1.0, pd.req.params, 0);
   s->queue.clear();
   s->n_active = 0;
   publish_locked(s);
@@ -827,6 +956,10 @@ void worker_main(fv2d_server *s) {
         std::lock_guard<std::mutex> lock(s->mu);
         publish_locked(s);
       }
+      if (const uint32_t lim = s->wait_limit_req.exchange(0)) {  // test hook (fv2d_server_set_tile_wait_limit)
+        s->h_ctl[1] = lim == UINT32_MAX ? 0u : lim;
+        cudaMemcpyAsync(s->d_ctl + 1, s->h_ctl + 1, sizeof(unsigned int), cudaMemcpyHostToDevice, s->stream);
+      }
       if (s->fault.empty()) run_once(s, s->cfg.steps_per_replay);
       if (s->fault.empty() && s->inject.exchange(false)) s->fault = "simulated failure (fv2d_server_inject_fault)";
       if (!s->fault.empty()) {
@@ -859,7 +992,7 @@ void autotune(fv2d_server *s) {
     double best = -1;
     int best_cfg = s->bucket_cfg[b];
     for (int c = 0; c < ncfg; ++c) {
-      if (!s->cfg_grid[c]) continue;
+      if (!s->cfg_grid[c] || cfg_ext(c)) continue;  // the common family's configurations
       s->bucket_cfg[b] = c;
       std::vector<int> used;
       for (int k = 0; k < nsims; ++k) {
@@ -905,7 +1038,7 @@ void autotune(fv2d_server *s) {
       cudaMemcpyAsync(s->d_sims, s->h_up, sizeof(SimDev) * s->max_sims, cudaMemcpyHostToDevice, s->stream);
       s->n_admitted = 0;
       s->n_active = 0;
-      for (int q = 0; q < kBuckets; ++q) s->items_in[q] = 0;
+      for (int q = 0; q < kLanes; ++q) s->items_in[q] = 0;
       s->lists_dirty = true;
     }
     s->bucket_cfg[b] = best_cfg;
@@ -922,7 +1055,7 @@ extern "C" {
 const char *fv2d_server_config_name(int index) {
   if (index < 0 || index >= batch_num_cfgs()) return nullptr;
   const char *name;
-  batch_cfg_info(index, nullptr, nullptr, nullptr, nullptr, nullptr, &name);
+  batch_cfg_info(index, nullptr, nullptr, nullptr, nullptr, nullptr, &name, nullptr);
   return name;
 }
 
@@ -949,13 +1082,15 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
             cudaMallocHost(&s->h_down, sizeof(SimDev) * s->max_sims) == cudaSuccess &&
             cudaMalloc(&s->d_tmaps, sizeof(CUtensorMap) * 2 * s->max_sims) == cudaSuccess &&
             cudaMallocHost(&s->h_tmaps, sizeof(CUtensorMap) * 2 * s->max_sims) == cudaSuccess &&
-            cudaMalloc(&s->d_nwork, sizeof(int) * kBuckets) == cudaSuccess &&
-            cudaMallocHost(&s->h_nwork, sizeof(int) * kBuckets) == cudaSuccess &&
+            cudaMalloc(&s->d_nwork, sizeof(int) * kLanes) == cudaSuccess &&
+            cudaMallocHost(&s->h_nwork, sizeof(int) * kLanes) == cudaSuccess &&
             cudaMalloc(&s->d_cons, sizeof(double) * kConsBlocks * 8 * s->max_sims) == cudaSuccess &&
+            cudaMalloc(&s->d_ctl, 2 * sizeof(unsigned int)) == cudaSuccess &&
+            cudaMallocHost(&s->h_ctl, 2 * sizeof(unsigned int)) == cudaSuccess &&
             cudaMallocHost(&s->h_cons, sizeof(double) * kConsBlocks * 8 * s->max_sims) == cudaSuccess &&
             cudaEventCreate(&s->ev0) == cudaSuccess && cudaEventCreate(&s->ev1) == cudaSuccess &&
             cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) == cudaSuccess;
-  for (int b = 0; ok && b < kBuckets; ++b)
+  for (int b = 0; ok && b < kLanes; ++b)
     ok = cudaStreamCreateWithFlags(&s->bstream[b], cudaStreamNonBlocking) == cudaSuccess &&
          cudaEventCreateWithFlags(&s->ev_join[b], cudaEventDisableTiming) == cudaSuccess;
   if (!ok) {
@@ -965,18 +1100,32 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   }
   std::memset(s->h_up, 0, sizeof(SimDev) * s->max_sims);
   cudaMemcpy(s->d_sims, s->h_up, sizeof(SimDev) * s->max_sims, cudaMemcpyHostToDevice);
-  std::memset(s->h_nwork, 0, sizeof(int) * kBuckets);
-  cudaMemcpy(s->d_nwork, s->h_nwork, sizeof(int) * kBuckets, cudaMemcpyHostToDevice);
+  s->h_ctl[0] = 0u;
+  s->h_ctl[1] = kTileWaitFinal;
+  cudaMemcpy(s->d_ctl, s->h_ctl, 2 * sizeof(unsigned int), cudaMemcpyHostToDevice);
+  std::memset(s->h_nwork, 0, sizeof(int) * kLanes);
+  cudaMemcpy(s->d_nwork, s->h_nwork, sizeof(int) * kLanes, cudaMemcpyHostToDevice);
   s->slots.resize(s->max_sims);
   for (int k = s->max_sims - 1; k >= 0; --k) s->free_slots.push_back(k);
   for (int c = 0; c < num_cfgs(); ++c) {
     int per_sm = 0;
     if (batch_setup(c, &per_sm) == cudaSuccess && per_sm > 0) s->cfg_grid[c] = per_sm * s->num_sms;
   }
-  if (cfg->tile_config > 0 && cfg->tile_config <= num_cfgs() && s->cfg_grid[cfg->tile_config - 1]) {
-    for (int b = 0; b < kBuckets; ++b) s->bucket_cfg[b] = cfg->tile_config - 1;
+  // the extended family: its first configuration that can run
+  for (int c = 0; c < num_cfgs() && s->ext_cfg < 0; ++c)
+    if (cfg_ext(c) && s->cfg_grid[c]) s->ext_cfg = c;
+  const int forced = cfg->tile_config - 1;
+  if (forced >= 0 && forced < num_cfgs() && s->cfg_grid[forced]) {
+    if (cfg_ext(forced))
+      s->ext_cfg = forced;
+    else
+      for (int b = 0; b < kBuckets; ++b) s->bucket_cfg[b] = forced;
   } else if (cfg->autotune) {
     autotune(s);
+  }
+  if (s->ext_cfg < 0) {  // no extended configuration can run on this device
+    fv2d_server_destroy(s);
+    return FV2D_ERR_CUDA;
   }
   publish_locked(s);  // no other thread yet
   s->worker = std::thread(worker_main, s);
@@ -992,7 +1141,7 @@ int fv2d_server_destroy(fv2d_server *s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (auto &g : s->graphs) cudaGraphExecDestroy(g.second);
   s->arena.free_all();
-  for (int b = 0; b < kBuckets; ++b) {
+  for (int b = 0; b < kLanes; ++b) {
     if (s->d_work[b]) cudaFree(s->d_work[b]);
     if (s->h_work[b]) cudaFreeHost(s->h_work[b]);
   }
@@ -1004,12 +1153,14 @@ int fv2d_server_destroy(fv2d_server *s) {
   if (s->d_nwork) cudaFree(s->d_nwork);
   if (s->h_nwork) cudaFreeHost(s->h_nwork);
   if (s->d_cons) cudaFree(s->d_cons);
+  if (s->d_ctl) cudaFree(s->d_ctl);
+  if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->h_cons) cudaFreeHost(s->h_cons);
   if (s->h_stage) cudaFreeHost(s->h_stage);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
-  for (int b = 0; b < kBuckets; ++b) {
+  for (int b = 0; b < kLanes; ++b) {
     if (s->ev_join[b]) cudaEventDestroy(s->ev_join[b]);
     if (s->bstream[b]) cudaStreamDestroy(s->bstream[b]);
   }
@@ -1030,7 +1181,8 @@ int fv2d_server_submit(fv2d_server *s, const fv2d_request *req, int64_t *id) {
   if (check_request(*req)) return FV2D_ERR_UNSUPPORTED;
   int pitch;
   long long plane;
-  if ((double)state_bytes(req->params.Nx, &pitch, &plane) > s->cfg.budget_bytes) return FV2D_ERR_SIZE;
+  size_t rows_off;
+  if ((double)state_bytes(req->params, &pitch, &plane, &rows_off) > s->cfg.budget_bytes) return FV2D_ERR_SIZE;
   std::lock_guard<std::mutex> lock(s->mu);
   if (s->broken) return FV2D_ERR_STATE;
   Pending pd;
@@ -1077,11 +1229,11 @@ int fv2d_server_get_prim(fv2d_server *s, int64_t id, double *q) {
     held = it->second;
   }
   const Finished &f = *held;
-  const int N = f.res.N;
-  const size_t n = (size_t)N * N;
+  const size_t n = (size_t)f.res.Nx * f.res.Ny;
   const double gm1 = f.gamma - 1.0;
   for (size_t c = 0; c < n; ++c) {
-    const double r = f.U[c], mu = f.U[n + c], mv = f.U[2 * n + c], E = f.U[3 * n + c];
+    const double r = (double)f.U[c] + f.bg_r, mu = f.U[n + c], mv = f.U[2 * n + c],
+                 E = (double)f.U[3 * n + c] + f.bg_e;
     const double u = mu / r, v = mv / r;
     q[4 * c] = r;
     q[4 * c + 1] = u;
@@ -1111,6 +1263,13 @@ int fv2d_server_inject_fault(fv2d_server *s) {
   return FV2D_OK;
 }
 
+int fv2d_server_set_tile_wait_limit(fv2d_server *s, uint32_t polls) {
+  if (!s) return FV2D_ERR_INVALID;
+  s->wait_limit_req.store(polls == 0 ? UINT32_MAX : polls);
+  s->cv.notify_all();
+  return FV2D_OK;
+}
+
 int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out) {
   if (!s || !out) return FV2D_ERR_INVALID;
   std::lock_guard<std::mutex> lock(s->mu);
@@ -1127,6 +1286,7 @@ int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out) {
   out->bytes_in_use = s->pub.bytes_in_use;
   out->bytes_reserved = s->pub.bytes_reserved;
   for (int b = 0; b < kBuckets; ++b) out->bucket_cfg[b] = s->bucket_cfg[b];
+  out->ext_cfg = s->ext_cfg;
   out->replays = s->pub.replays;
   return FV2D_OK;
 }

@@ -24,7 +24,7 @@ class Result(C.Structure):
     _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("steps", C.c_int32), ("t", C.c_double),
                 ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
                 ("cons0", C.c_double * 4), ("cons1", C.c_double * 4), ("negatives", C.c_uint64),
-                ("N", C.c_int32), ("bucket", C.c_int32)]
+                ("Nx", C.c_int32), ("Ny", C.c_int32), ("bucket", C.c_int32), ("lane", C.c_int32)]
 
     def as_dict(self):
         d = {n: getattr(self, n) for n, _ in self._fields_}
@@ -38,7 +38,7 @@ class Stats(C.Structure):
                 ("failed", C.c_int64), ("active", C.c_int32), ("queued", C.c_int32),
                 ("cell_updates", C.c_double), ("busy_s", C.c_double), ("bytes_in_use", C.c_double),
                 ("bytes_reserved", C.c_double), ("bucket_cfg", C.c_int32 * 4), ("replays", C.c_int32),
-                ("pad", C.c_int32)]
+                ("ext_cfg", C.c_int32)]
 
 
 def _bind(L):
@@ -56,6 +56,7 @@ def _bind(L):
     L.fv2d_server_last_error.argtypes = [vp, C.c_char_p, C.c_int]
     L.fv2d_server_check_request.argtypes = [C.POINTER(Request), C.c_char_p, C.c_int]
     L.fv2d_server_inject_fault.argtypes = [vp]
+    L.fv2d_server_set_tile_wait_limit.argtypes = [vp, C.c_uint32]
     L.fv2d_server_config_name.argtypes = [C.c_int]
     L.fv2d_server_config_name.restype = C.c_char_p
     L._serve_bound = True
@@ -137,7 +138,7 @@ class Server:
         if rc != 0:
             why = check_request(r)
             raise ValueError(f"request rejected ({rc}{': ' + why if why else ''})")
-        self._n[i.value] = params.Nx
+        self._n[i.value] = (params.Ny, params.Nx)
         return i.value
 
     def poll(self, max_results=1024):
@@ -161,9 +162,14 @@ class Server:
         """Test hook: the worker stops as if a CUDA call had failed."""
         self.L.fv2d_server_inject_fault(self.h)
 
+    def set_tile_wait_limit(self, polls):
+        """Test hook: polls of a TMA tile copy's barrier before the request
+        it belongs to is failed (default 2^24; 0 = none)."""
+        self.L.fv2d_server_set_tile_wait_limit(self.h, int(polls))
+
     def get_prim(self, rid):
-        N = self._n[rid]
-        q = np.empty((N, N, 4))
+        ny, nx = self._n[rid]
+        q = np.empty((ny, nx, 4))
         rc = self.L.fv2d_server_get_prim(self.h, rid, q.ctypes.data_as(C.POINTER(C.c_double)))
         if rc != 0:
             raise KeyError(rid)

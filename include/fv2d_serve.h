@@ -5,20 +5,25 @@
  *
  * No counterpart in the reference (which runs one simulation per process,
  * main.cpp:13-101); each simulation follows the reference's step
- * (ComputeDt.h:18-65, Update.h:93-191, SimInfo.h:576-646) in binary32
- * storage and flux arithmetic, with the simulation clock, dt, the
- * conservation sums and (for low-Mach requests) the internal-energy
- * recovery E - rho|u|^2/2 in binary64.
+ * (ComputeDt.h:18-65, Update.h:93-222, SimInfo.h:576-646) -- every Riemann
+ * solver, reconstruction (and the MUSCL-Hancock extension), time stepping,
+ * gravity, conduction and viscosity setting of fv2d_params, on any Nx x Ny
+ * grid -- in binary32 storage and flux arithmetic, with the simulation clock,
+ * dt, the conservation sums and (for low-Mach requests) the internal-energy
+ * recovery E - rho|u|^2/2 in binary64.  The state is stored as its offset
+ * from a per-request background density and total energy (the medians of the
+ * initial condition), which keeps more digits where the flow stays near it.
  *
  * Serving model:
  *   - fv2d_server_submit queues a request; a worker thread admits queued
  *     requests (first in, first out, smaller ones may pass a request that
  *     does not fit) while the HBM budget and the simulation table allow;
  *   - every admitted state stays resident in HBM until it completes;
- *   - all admitted simulations advance together: per grid-size bucket one
- *     persistent kernel launch per step walks a (simulation, tile) work list,
- *     each simulation reduces its own dt; a CUDA graph replays several steps
- *     between admissions and retirements;
+ *   - all admitted simulations advance together: per lane (grid-size bucket
+ *     of one kernel family) one persistent kernel launch per stage walks a
+ *     (simulation, tile) work list, each simulation reduces its own dt; an
+ *     SSP-RK2 step takes two launches; a CUDA graph replays several launches
+ *     between admissions and retirements, the lanes as parallel branches;
  *   - tile shape, threads per tile and halo staging are chosen per bucket by
  *     an autotuner at start-up (or fixed defaults).
  * A simulation's result does not depend on what else was in the batch.
@@ -64,8 +69,7 @@ typedef struct fv2d_server_config {
 typedef struct fv2d_request {
   uint32_t struct_size;
   int32_t problem;   /* FV2D_PB_* initial condition */
-  fv2d_params params;/* Nx == Ny == N (multiple of 32, 64..4096); PCM or PLM; HLL or HLLC; Euler;
-                        constant gravity, constant conductivity and viscosity allowed */
+  fv2d_params params;/* any valid parameter block with 16 <= Nx, Ny <= 8192 */
   int32_t max_steps; /* stop after this many steps */
   int32_t lowmach;   /* 1: recover the pressure from E - rho|u|^2/2 in binary64 where it cancels */
   double tend;       /* also stop once t + epsilon >= tend (<= 0: no time limit) */
@@ -73,15 +77,17 @@ typedef struct fv2d_request {
 
 typedef struct fv2d_result {
   int64_t id;
-  int32_t status;    /* FV2D_OK, or FV2D_ERR_NUMERIC when the dt guard stopped it */
+  int32_t status;    /* FV2D_OK; FV2D_ERR_NUMERIC when the NaN / dt guard stopped it; FV2D_ERR_CUDA when a
+                        tile copy outlived its bounded wait (fv2d_server_set_tile_wait_limit) */
   int32_t steps;     /* steps taken */
   double t;          /* simulation time reached (binary64 clock) */
   double submit_s, admit_s, done_s;  /* server clock, seconds since fv2d_server_create */
   double cons0[4];   /* sum over cells of (rho, rho u, rho v, E) * dx * dy at admission, */
   double cons1[4];   /* and at completion: compensated binary64 sums of the binary32 state */
   uint64_t negatives;/* cells reset by the negative density/pressure guard */
-  int32_t N;
-  int32_t bucket;
+  int32_t Nx, Ny;
+  int32_t bucket;    /* grid-size bucket (0..3) */
+  int32_t lane;      /* bucket, + 4 when the extended kernel family ran it */
 } fv2d_result;
 
 typedef struct fv2d_server_stats {
@@ -91,9 +97,9 @@ typedef struct fv2d_server_stats {
   double busy_s;         /* wall time with at least one active simulation */
   double bytes_in_use;   /* HBM held by resident states */
   double bytes_reserved; /* HBM reserved by the state arena */
-  int32_t bucket_cfg[4]; /* configuration index chosen per bucket (see fv2d_server_config_name) */
+  int32_t bucket_cfg[4]; /* common-family configuration index per bucket (see fv2d_server_config_name) */
   int32_t replays;       /* graph replays launched */
-  int32_t pad;
+  int32_t ext_cfg;       /* extended-family configuration index */
 } fv2d_server_stats;
 
 int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out);
@@ -117,7 +123,7 @@ int fv2d_server_poll(fv2d_server *s, fv2d_result *out, int max, int *n);
  * service has stopped (see Failures above). */
 int fv2d_server_drain(fv2d_server *s, double timeout_s);
 
-/* Final primitive state of a completed request (N x N x {rho,u,v,p}, binary64
+/* Final primitive state of a completed request (Ny x Nx x {rho,u,v,p}, binary64
  * values of the binary32 state), until fv2d_server_release. */
 int fv2d_server_get_prim(fv2d_server *s, int64_t id, double *q_host);
 int fv2d_server_release(fv2d_server *s, int64_t id);
@@ -131,6 +137,15 @@ int fv2d_server_last_error(fv2d_server *s, char *buf, int len);
 /* Test hook for the failure path above, with no GPU fault: the worker stops
  * after its current replay as if a CUDA call had failed. */
 int fv2d_server_inject_fault(fv2d_server *s);
+
+/* Test hook for the bounded tile-copy wait, with no GPU fault: the served
+ * kernels that stage tiles by TMA poll a copy's barrier at most `polls` times
+ * (default 2^24; 0 = not at all) before they fail the simulation the tile
+ * belongs to (its result completes with FV2D_ERR_CUDA) and wait once more,
+ * bounded, for the copy to land before the tile buffer is used again.  A copy
+ * that outlives that second wait stops the service as a failed CUDA call
+ * does.  Applied by the worker before its next replay. */
+int fv2d_server_set_tile_wait_limit(fv2d_server *s, uint32_t polls);
 
 /* Name of tile configuration `index` ("32x16/256/tma", ...); NULL if none. */
 const char *fv2d_server_config_name(int index);

@@ -917,6 +917,23 @@ int fv2d_oracle_update(fv2d_oracle *o, double dt) {
   return FV2D_OK;
 }
 
+int fv2d_oracle_round_cons_f32(fv2d_oracle *o, const double *bg) {
+  if (!o) return FV2D_ERR_INVALID;
+  const Grid &g = o->g;
+  const double zero[4] = {0.0, 0.0, 0.0, 0.0};
+  const double *b = bg ? bg : zero;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < g.Nty; ++j)
+    for (int i = 0; i < g.Ntx; ++i)
+      for (int v = 0; v < 4; ++v) {
+        double &x = o->U[o->at(j, i, v)];
+        x = (double)(float)(x - b[v]) + b[v];
+      }
+  consToPrimGrid(o, o->U);
+  checkNegatives(o);
+  return FV2D_OK;
+}
+
 int fv2d_oracle_get_counters(const fv2d_oracle *o, uint64_t out[3]) {
   if (!o || !out) return FV2D_ERR_INVALID;
   for (int k = 0; k < 3; ++k) out[k] = o->counters[k];

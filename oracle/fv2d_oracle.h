@@ -55,6 +55,14 @@ int fv2d_oracle_compute_dt(const fv2d_oracle *o, double out[4]);
  * checkNegatives(Q). */
 int fv2d_oracle_update(fv2d_oracle *o, double dt);
 
+/* Accuracy-floor hook (no counterpart in the reference): rounds every stored
+ * conservative value (ghosts included) to binary32 as the offset U - bg[v]
+ * from a constant background (bg may be NULL for zero), then rebuilds Q with
+ * consToPrim and checkNegatives.  Called after each update, it gives a run in
+ * binary64 arithmetic whose state is stored the way a binary32 service stores
+ * it: the error that storage alone causes. */
+int fv2d_oracle_round_cons_f32(fv2d_oracle *o, const double *bg);
+
 /* Counters of the last checkNegatives: {negative density, negative
  * pressure, NaN count} (SimInfo.h:602-646). */
 int fv2d_oracle_get_counters(const fv2d_oracle *o, uint64_t out[3]);

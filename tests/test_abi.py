@@ -165,9 +165,15 @@ def test_server_request_checks_without_a_server(libs):
     assert check_request(req()) == ""
     buf = C.create_string_buffer(64)
     assert lib.fv2d_server_check_request(C.byref(req()), buf, 64) == _abi.OK
-    cases = [(dict(riemann_solver=fv.FSLP), "HLL and HLLC"), (dict(Nx=100, Ny=100), "multiple of 32"),
-             (dict(Ny=96), "square"), (dict(time_stepping=fv.TS_RK2), "Euler"),
-             (dict(reconstruction=fv.MUSCL_HANCOCK), "PCM and PLM")]
+    # every scheme, physics switch and rectangular grid is accepted
+    for kw in (dict(riemann_solver=fv.FSLP), dict(Nx=100, Ny=36), dict(Ny=96), dict(time_stepping=fv.TS_RK2),
+               dict(reconstruction=fv.MUSCL_HANCOCK), dict(gravity_mode=fv.GRAV_ANALYTICAL),
+               dict(well_balanced_flux_at_y_bc=1), dict(thermal_conductivity_active=1, kappa=1e-3,
+                                                        thermal_conductivity_mode=fv.TCM_B02,
+                                                        bctc_ymin=fv.BCTC_FIXED_TEMPERATURE)):
+        assert check_request(req(**kw)) == "", kw
+    cases = [(dict(Nx=8), "[16, 8192]"), (dict(Ny=8193), "[16, 8192]"), (dict(reconstruction=9), "reconstruction"),
+             (dict(riemann_solver=3), "riemann_solver")]
     for kw, why in cases:
         r = req(**kw)
         assert lib.fv2d_server_check_request(C.byref(r), buf, 64) == _abi.ERR_UNSUPPORTED, kw
@@ -175,6 +181,9 @@ def test_server_request_checks_without_a_server(libs):
     bad = req()
     bad.struct_size -= 8
     assert "struct_size" in check_request(bad)
+    neg = req()
+    neg.max_steps = -1
+    assert "max_steps" in check_request(neg)
     assert lib.fv2d_server_check_request(None, buf, 64) == _abi.ERR_INVALID
     assert lib.fv2d_server_check_request(C.byref(req()), None, 0) == _abi.OK
     assert lib.fv2d_server_check_request(C.byref(req()), buf, -1) == _abi.ERR_INVALID

@@ -73,21 +73,10 @@ def test_single_rank_helpers():
     assert bench.whole_job_rate(10.0, 1, 2.0) == 5.0
 
 
-def test_binary32_rounded_state_matches_the_stored_conservative_state():
-    import numpy as np
+def test_checkpoints_of_the_error_curves():
     sys.path.insert(0, REPO)
     import bench
-    rng = np.random.default_rng(5)
-    q = np.stack([rng.uniform(0.1, 2.0, (6, 7)), rng.uniform(-1, 1, (6, 7)), rng.uniform(-1, 1, (6, 7)),
-                  rng.uniform(0.1, 3.0, (6, 7))], axis=-1)
-    g = 1.4
-    q2 = bench.binary32_rounded_state(q, g)
-
-    def cons(x):
-        r, u, v, p = (x[..., k] for k in range(4))
-        return np.stack([r, r * u, r * v, p / (g - 1.0) + 0.5 * r * (u * u + v * v)], axis=-1)
-    # the conservative state of the result is the binary32 rounding of q's
-    assert np.allclose(cons(q2), cons(q).astype(np.float32).astype(np.float64), rtol=1e-13, atol=1e-15)
-    assert np.array_equal(q2[..., 0], q[..., 0].astype(np.float32).astype(np.float64))
-    rel = np.abs(q2 - q) / np.maximum(np.abs(q), 1e-30)
-    assert 0 < rel.max() < 1e-6
+    assert bench.checkpoints(800) == [100, 200, 300, 400, 500, 600, 700, 800]
+    assert bench.checkpoints(3) == [1, 2, 3]
+    pts = bench.checkpoints(1637)
+    assert pts[-1] == 1637 and len(pts) == 8 and pts == sorted(set(pts))

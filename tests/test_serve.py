@@ -1,6 +1,10 @@
 """The batched FP32 service (include/fv2d_serve.h), through the C-ABI.
 
-* A request's result is identical (bit for bit) alone and in a mixed batch.
+* A request's result is identical (bit for bit) alone and in a mixed batch,
+  for both kernel families (the common one, and the extended one with FSLP,
+  MUSCL-Hancock, analytical gravity, B02 conductivity, the y-boundary
+  conduction modes and the well-balanced y flux), Euler and SSP-RK2, square
+  and rectangular grids.
 * Accuracy against the binary64 plain path (bit-identical to the reference):
   L1 relative error of rho and p after the same number of steps, and the
   conservation drift of the binary64 sums.
@@ -24,6 +28,42 @@ def params(N, **kw):
     return fv.default_params(**base)
 
 
+def rt_rect(nx=64, ny=192, **kw):
+    """The Rayleigh-Taylor benchmark set-up on a reduced rectangle: HLL,
+    constant gravity, conduction and viscosity, periodic x, reflecting y."""
+    import fv2d_gb300 as fv
+    base = dict(Ny=ny, riemann_solver=fv.HLL, boundary_x=fv.BC_PERIODIC, xmax=0.5, ymax=1.5,
+                gravity_mode=fv.GRAV_CONSTANT, gy=-0.1, thermal_conductivity_active=1, kappa=1e-4,
+                viscosity_active=1, mu=1e-4)
+    base.update(kw)
+    return params(nx, **base)
+
+
+def c91_small():
+    """The reference's C91 set-up (settings/C91.ini) on 64 x 32: PCM_WB,
+    well-balanced y flux, constant gravity, conduction with the fixed
+    temperature / fixed gradient y-boundary modes, viscosity."""
+    import fv2d_gb300 as fv
+    f = fv.as_float32
+    return params(64, Ny=32, xmax=8.0, ymax=4.0, gamma0=f(1.66666667), CFL=f(0.1), reconstruction=fv.PCM_WB,
+                  well_balanced_flux_at_y_bc=1, gravity_mode=fv.GRAV_CONSTANT, gy=40.0,
+                  thermal_conductivity_active=1, kappa=f(0.07), bctc_ymin=fv.BCTC_FIXED_TEMPERATURE,
+                  bctc_ymin_value=1.0, bctc_ymax=fv.BCTC_FIXED_GRADIENT, bctc_ymax_value=10.0,
+                  viscosity_active=1, mu=f(0.0028), c91_pert=f(1e-3), theta1=20.0)
+
+
+def h84_b02_small():
+    """H84 on 80 x 20 with B02 conductivity and the analytical (hot-bubble)
+    gravity: the per-row tables of the extended family."""
+    import fv2d_gb300 as fv
+    f = fv.as_float32
+    return params(80, Ny=20, xmax=4.0, ymin=2.0, ymax=3.0, gamma0=f(1.66666667), CFL=f(0.1),
+                  boundary_x=fv.BC_PERIODIC, gravity_mode=fv.GRAV_ANALYTICAL, hot_bubble_g0=2.0,
+                  thermal_conductivity_active=1, thermal_conductivity_mode=fv.TCM_B02, kappa=f(0.0071),
+                  b02_ymid=2.5, b02_kappa1=1.0, b02_kappa2=0.5, b02_thickness=0.1,
+                  viscosity_active=1, mu=f(0.0028), h84_pert=f(1e-4))
+
+
 def mixed_requests():
     import fv2d_gb300 as fv
     return [
@@ -32,9 +72,16 @@ def mixed_requests():
         ("kh_step", params(96, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC, seed=7), 50, False),
         ("gresho_vortex", params(64, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC,
                                  gresho_Mach=fv.as_float32(0.05)), 100, True),
-        ("rt_hydrostatic", params(160, riemann_solver=fv.HLL, boundary_x=fv.BC_PERIODIC, xmax=0.5, ymax=1.5,
-                                  gravity_mode=fv.GRAV_CONSTANT, gy=-0.1, thermal_conductivity_active=1,
-                                  kappa=1e-4, viscosity_active=1, mu=1e-4), 40, False),
+        ("rt_hydrostatic", rt_rect(), 40, False),
+        # SSP-RK2 in the common family, rectangular
+        ("kh_step", params(128, Ny=96, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC, seed=3,
+                           time_stepping=fv.TS_RK2), 30, False),
+        # the extended family
+        ("sod_x", params(160, Ny=40, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC,
+                         reconstruction=fv.MUSCL_HANCOCK), 70, False),
+        ("rt_hydrostatic", rt_rect(48, 144, riemann_solver=fv.FSLP, time_stepping=fv.TS_RK2), 25, False),
+        ("C91", c91_small(), 40, False),
+        ("H84", h84_b02_small(), 40, False),
     ]
 
 
@@ -56,6 +103,8 @@ def test_same_result_alone_and_in_the_mix(gpu_lib, tile, active):
             assert s.drain(120) == 0
             res = {r.id: r for r in s.poll()}
             assert res[rid].status == 0 and res[rid].steps == n
+            assert (res[rid].Nx, res[rid].Ny) == (p.Nx, p.Ny)
+            assert res[rid].lane >= 4 if k_ext(p) else res[rid].lane < 4
             alone.append((s.get_prim(rid), res[rid].t))
     with Server(budget_bytes=4e9, autotune=False, tile_config=tile, active_cells=active) as s:
         fillers = [s.submit("sedov", params(N), 30 + N // 16) for N in (64, 320, 512, 192, 96)]
@@ -68,6 +117,14 @@ def test_same_result_alone_and_in_the_mix(gpu_lib, tile, active):
             q, t = alone[k]
             assert res[rid].t == t, reqs[k][0]
             assert bits_equal(s.get_prim(rid), q), reqs[k][0]
+
+
+def k_ext(p):
+    """Whether a request runs in the extended kernel family."""
+    import fv2d_gb300 as fv
+    return (p.riemann_solver == fv.FSLP or p.reconstruction == fv.MUSCL_HANCOCK
+            or p.gravity_mode == fv.GRAV_ANALYTICAL or p.well_balanced_flux_at_y_bc
+            or (p.thermal_conductivity_active and (p.thermal_conductivity_mode != 0 or p.bctc_ymin or p.bctc_ymax)))
 
 
 def l1_rel(a, b):
@@ -86,6 +143,15 @@ def test_accuracy_against_fp64_path(gpu_lib, tile):
         ("kh_step", params(256, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC), 200, False),
         ("gresho_vortex", params(128, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC,
                                  gresho_Mach=fv.as_float32(0.1)), 200, True),
+        ("rt_hydrostatic", rt_rect(), 200, False),
+        ("kh_step", params(192, Ny=128, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC,
+                           time_stepping=fv.TS_RK2), 100, False),
+        ("sod_x", params(256, Ny=32, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC,
+                         reconstruction=fv.MUSCL_HANCOCK), 200, False),
+        ("sod_x", params(256, Ny=32, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC, riemann_solver=fv.FSLP,
+                         time_stepping=fv.TS_RK2), 200, False),
+        ("C91", c91_small(), 100, False),
+        ("H84", h84_b02_small(), 100, False),
     ]
     report = {}
     with Server(budget_bytes=4e9, autotune=False, tile_config=tile) as s:
@@ -100,14 +166,51 @@ def test_accuracy_against_fp64_path(gpu_lib, tile):
             q32 = s.get_prim(rid)
             r = res[rid]
             drift = abs(r.cons1[0] - r.cons0[0]) / abs(r.cons0[0])
-            report[pb] = (l1_rel(q32[..., 0], q64[..., 0]), l1_rel(q32[..., 3], q64[..., 3]), drift)
+            report[f"{pb}/{p.Nx}x{p.Ny}/rs{p.riemann_solver}/rc{p.reconstruction}/ts{p.time_stepping}"] = (
+                l1_rel(q32[..., 0], q64[..., 0]), l1_rel(q32[..., 3], q64[..., 3]), drift)
             sim.close()
     print(report)
-    for pb, (erho, ep, drift) in report.items():
-        assert erho < 1e-4 and ep < 1e-4, (pb, erho, ep)
+    # 1e-5 in rho for the problems that do not amplify perturbations over
+    # these step counts; the Gresho vortex (whose binary64 run grows a
+    # checkerboard pressure mode) and Rayleigh-Taylor (a physical
+    # instability) within a few times that
+    for key, (erho, ep, drift) in report.items():
+        kind = key.split("/")[0]
+        tol = {"gresho_vortex": 3e-5, "rt_hydrostatic": 1e-4}.get(kind, 1e-5)
+        assert erho < tol and ep < 3 * tol, (key, erho, ep)
     # closed domains conserve mass to binary32 rounding of the state
-    for pb in ("sedov", "kh_step", "gresho_vortex"):
-        assert report[pb][2] < 1e-6, (pb, report[pb])
+    for key, v in report.items():
+        if key.split("/")[0] in ("sedov", "kh_step", "gresho_vortex", "C91"):
+            assert v[2] < 1e-6, (key, v)
+
+
+def test_tile_copy_wait_limit_fails_only_its_request(gpu_lib):
+    """The bounded wait of the TMA-staged kernel, with no GPU fault: with a
+    wait limit of zero polls every tile copy outlives its first wait, so the
+    request completes with FV2D_ERR_CUDA (the copy itself lands during the
+    second, bounded wait); the service keeps serving, and with the default
+    limit the next request gives its stand-alone result."""
+    from fv2d_gb300._abi import ERR_CUDA
+    from fv2d_gb300.serve import Server
+    tile = "32x16/256/tma"
+    with Server(budget_bytes=1e9, autotune=False, tile_config=tile) as s:
+        rid = s.submit("sedov", params(128), 20)
+        assert s.drain(60) == 0
+        assert [r.status for r in s.poll()] == [0]
+        alone = s.get_prim(rid)
+    with Server(budget_bytes=1e9, autotune=False, tile_config=tile) as s:
+        s.set_tile_wait_limit(0)
+        bad = s.submit("sedov", params(128), 20)
+        assert s.drain(60) == 0
+        res = {r.id: r for r in s.poll()}
+        assert res[bad].status == ERR_CUDA
+        s.set_tile_wait_limit(1 << 24)
+        good = s.submit("sedov", params(128), 20)
+        assert s.drain(60) == 0
+        res = {r.id: r for r in s.poll()}
+        assert res[good].status == 0 and res[good].steps == 20
+        assert bits_equal(s.get_prim(good), alone)
+        assert s.last_error() == ""
 
 
 def test_admission_respects_budget(gpu_lib):
@@ -136,12 +239,13 @@ def test_rejects_unsupported_requests(gpu_lib):
     import fv2d_gb300 as fv
     from fv2d_gb300.serve import Server
     with Server(budget_bytes=1e9, autotune=False) as s:
-        for bad in (dict(time_stepping=fv.TS_RK2), dict(riemann_solver=fv.FSLP), dict(Ny=96),
-                    dict(reconstruction=fv.MUSCL_HANCOCK)):
+        for bad in (dict(Nx=8), dict(Ny=9000), dict(Nx=8200, Ny=16), dict(reconstruction=7)):
             with pytest.raises(ValueError):
                 s.submit("sedov", params(128, **bad), 10)
         with pytest.raises(ValueError):
-            s.submit("sedov", params(100), 10)  # not a multiple of 32
+            s.submit(55, params(128), 10)  # unknown problem
+        with pytest.raises(ValueError):
+            s.submit("sedov", params(128), -1)
         # argument checks of the C entry points
         import ctypes as C
         from fv2d_gb300._abi import ERR_INVALID
