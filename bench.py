@@ -289,7 +289,8 @@ def served_accuracy(fv, sample_every=16, device=0):
     pts = {i: checkpoints(reqs[i]["steps"]) for i in sub}
     q32 = {}
     res = {}
-    with Server(budget_bytes=100e9, device=device, autotune=False) as srv:
+    # the kernel configurations the service runs in production (autotuned)
+    with Server(budget_bytes=100e9, device=device, autotune=True) as srv:
         ids = {}
         for i in sub:
             for n in pts[i]:

@@ -184,6 +184,32 @@ def test_accuracy_against_fp64_path(gpu_lib, tile):
             assert v[2] < 1e-6, (key, v)
 
 
+@pytest.mark.parametrize("tile", TILES)
+@pytest.mark.parametrize("variant", ["plm", "rk2", "muscl_hancock"])
+def test_one_dimensional_problems_stay_one_dimensional(gpu_lib, tile, variant):
+    """A Sod tube along x with periodic y (every row the same) and one along
+    y with periodic x: every row (column) stays bitwise the same and the
+    transverse velocity exactly zero, which holds only if each face shared
+    by two work items (band and strip boundaries) gets the same flux from
+    both.  Grids that cut work items unevenly."""
+    import fv2d_gb300 as fv
+    from fv2d_gb300.serve import Server
+    kw = {"plm": {}, "rk2": dict(time_stepping=fv.TS_RK2),
+          "muscl_hancock": dict(reconstruction=fv.MUSCL_HANCOCK)}[variant]
+    cases = [("sod_x", params(96, Ny=100, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC, **kw)),
+             ("sod_y", params(70, Ny=90, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_ABSORBING, **kw))]
+    with Server(budget_bytes=1e9, autotune=False, tile_config=tile) as s:
+        ids = [s.submit(pb, p, 300) for pb, p in cases]
+        assert s.drain(120) == 0
+        res = {r.id: r for r in s.poll()}
+        qx, qy = s.get_prim(ids[0]), s.get_prim(ids[1])
+    assert all(res[i].status == 0 for i in ids)
+    assert np.array_equal(qx, np.broadcast_to(qx[:1], qx.shape)) and np.all(qx[..., 2] == 0.0)
+    assert np.array_equal(qy, np.broadcast_to(qy[:, :1], qy.shape)) and np.all(qy[..., 1] == 0.0)
+    # the waves have moved
+    assert np.ptp(qx[0, :, 1]) > 0.1 and np.ptp(qy[:, 0, 2]) > 0.1
+
+
 def test_tile_copy_wait_limit_fails_only_its_request(gpu_lib):
     """The bounded wait of the TMA-staged kernel, with no GPU fault: with a
     wait limit of zero polls every tile copy outlives its first wait, so the
