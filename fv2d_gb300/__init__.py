@@ -51,6 +51,7 @@ def lib():
         L.fv2d_set_stream.argtypes = [vp, vp]
         L.fv2d_init_problem.argtypes = [vp, C.c_int]
         L.fv2d_set_prim.argtypes = [vp, _dp]
+        L.fv2d_prefetch_prim.argtypes = [vp, vp]
         L.fv2d_get_prim.argtypes = [vp, _dp]
         L.fv2d_get_cons.argtypes = [vp, _dp]
         L.fv2d_set_prim_device.argtypes = [vp, vp]
@@ -193,6 +194,12 @@ class Simulation:
     def set_prim_ptr(self, host_ptr):
         """set_prim from a host address (page-locked memory is read by the device directly)."""
         self._check(self._lib.fv2d_set_prim(self.h, C.cast(C.c_void_p(host_ptr), _dp)))
+
+    def prefetch_prim_ptr(self, host_ptr):
+        """Start copying the next input (page-locked host address) into the
+        staging buffer while queued work runs; the next set_prim_ptr with
+        the same address builds the state from it."""
+        self._check(self._lib.fv2d_prefetch_prim(self.h, C.c_void_p(host_ptr)))
 
     def get_prim_ptr(self, host_ptr):
         """get_prim into a host address (the registered host mirror is returned without a copy)."""

@@ -43,12 +43,19 @@ struct fv2d_ctx {
   double *Q[2] = {nullptr, nullptr};
   double *U = nullptr, *U1 = nullptr;
   double *stage = nullptr;  // interleaved interior staging (Ny*Nx*4)
+  // fv2d_prefetch_prim: a copy of the next input into `stage` on its own
+  // stream, overlapping the work on `stream`
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_stage_free = nullptr;  // recorded on `stream` after each of its uses of `stage`
+  cudaEvent_t ev_prefetch = nullptr;    // recorded on copy_stream after the prefetch copy
+  const double *prefetched = nullptr;   // host array the pending prefetch copies (null: none)
   float *grav_row = nullptr;
   double *kap_row = nullptr;
   double *log = nullptr;
   int log_cap = 0;
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // page-locked mirror for readbacks
+  bool st_fresh = false;        // st_host equals st: read back with no work queued since
   CUtensorMap tm[2];
   StepArgs args;
   double inv_tc = 0, inv_visc = 0;
@@ -73,6 +80,18 @@ int fail(fv2d_ctx *c, int code, const std::string &msg) {
 int cuda_fail(fv2d_ctx *c, cudaError_t e, const char *what) {
   return fail(c, FV2D_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
+
+// The staging buffer is shared by the context's stream and the prefetch
+// copy: before the stream uses it, a pending prefetch is waited for (and its
+// data dropped); after the stream's use, an event tells the next prefetch
+// when it may write.
+void stage_take(fv2d_ctx *c) {
+  if (c->prefetched) {
+    cudaStreamWaitEvent(c->stream, c->ev_prefetch, 0);
+    c->prefetched = nullptr;
+  }
+}
+void stage_release(fv2d_ctx *c) { cudaEventRecord(c->ev_stage_free, c->stream); }
 #define CK(call)                                              \
   do {                                                        \
     cudaError_t e_ = (call);                                  \
@@ -228,8 +247,12 @@ __global__ void begin_kernel(DevState *st, double tend, double next_save, double
 int sync_state(fv2d_ctx *ctx) {
   CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->st_fresh = true;
   return FV2D_OK;
 }
+// The device state as the host last read it, read again only when work has
+// been queued since (a set_prim followed by compute_dt needs one round trip).
+int fresh_state(fv2d_ctx *ctx) { return ctx->st_fresh ? FV2D_OK : sync_state(ctx); }
 
 void fill_args(fv2d_ctx *c) {
   const fv2d_params &p = c->p;
@@ -291,6 +314,7 @@ int recon_kind(int r) {
 }
 
 int launch_update(fv2d_ctx *ctx, int driven, double dt) {
+  ctx->st_fresh = false;
   StepArgs a = ctx->args;
   a.driven = driven;
   a.dt_arg = dt;
@@ -324,7 +348,7 @@ const double *mapped_host(const double *p) {
 
 int run_prepare(fv2d_ctx *ctx, const double *src) {
   const fv2d_params &p = ctx->p;
-  sync_state(ctx);  // reads the parity of the current buffer
+  if (int rc = fresh_state(ctx)) return rc;  // the parity of the current buffer
   ctx->mirror_valid = false;
   PrepArgs pa;
   std::memset(&pa, 0, sizeof(pa));
@@ -354,6 +378,7 @@ int run_prepare(fv2d_ctx *ctx, const double *src) {
   pa.inv_visc = ctx->inv_visc;
   pa.bcx = p.boundary_x;
   pa.bcy = p.boundary_y;
+  ctx->st_fresh = false;
   prepare_kernel<<<nb, 256, 0, ctx->stream>>>(pa);
   CK(cudaGetLastError());
   ctx->have_state = true;
@@ -403,6 +428,10 @@ int ensure_graph(fv2d_ctx *ctx) {
 }
 
 void free_all(fv2d_ctx *c) {
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+  if (c->ev_stage_free) cudaEventDestroy(c->ev_stage_free);
+  if (c->ev_prefetch) cudaEventDestroy(c->ev_prefetch);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (double *ptr : {c->Q[0], c->Q[1], c->U, c->U1, c->stage, c->kap_row, c->log})
     if (ptr) cudaFree(ptr);
@@ -460,7 +489,10 @@ int fv2d_create(const fv2d_params *p, int device, fv2d_ctx **out) {
   }
   cudaGetDevice(&ctx->device);
   if ((e = init_step_kernels()) != cudaSuccess) return bail(cuda_fail(ctx, e, "step kernel attributes"));
-  if ((e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+  if ((e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&ctx->ev_stage_free, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&ctx->ev_prefetch, cudaEventDisableTiming)) != cudaSuccess)
     return bail(cuda_fail(ctx, e, "cudaStreamCreate"));
   ctx->stream = ctx->own_stream;
 
@@ -542,24 +574,51 @@ int fv2d_set_stream(fv2d_ctx *ctx, void *stream) {
 int fv2d_set_prim_device(fv2d_ctx *ctx, const double *q_dev) {
   if (!ctx || !q_dev) return FV2D_ERR_INVALID;
   const size_t n = (size_t)ctx->p.Nx * ctx->p.Ny * 4;
+  stage_take(ctx);
   CK(cudaMemcpyAsync(ctx->stage, q_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  return run_prepare(ctx, ctx->stage);
+  const int rc = run_prepare(ctx, ctx->stage);
+  stage_release(ctx);
+  return rc;
 }
 
 int fv2d_set_prim(fv2d_ctx *ctx, const double *q_host) {
   const fv2d::NvtxRange nvtx_range("fv2d_set_prim");
   if (!ctx || !q_host) return FV2D_ERR_INVALID;
-  // Page-locked host memory is read by the set-up kernel itself over the
-  // host link (one pass instead of a copy then a pass); pageable memory is
-  // copied to the staging buffer first.
-  const double *src = mapped_host(q_host);
-  if (!src) {
+  // A prefetched copy of q_host (fv2d_prefetch_prim) is converted from the
+  // staging buffer.  Otherwise page-locked host memory is read by the set-up
+  // kernel itself over the host link (one pass instead of a copy then a
+  // pass); pageable memory is copied to the staging buffer first.
+  const double *src = nullptr;
+  bool staged = false;
+  if (ctx->prefetched == q_host) {
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_prefetch, 0));
+    ctx->prefetched = nullptr;
+    src = ctx->stage;
+    staged = true;
+  } else if (!(src = mapped_host(q_host))) {
     const size_t n = (size_t)ctx->p.Nx * ctx->p.Ny * 4;
+    stage_take(ctx);
     CK(cudaMemcpyAsync(ctx->stage, q_host, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     src = ctx->stage;
+    staged = true;
   }
-  if (int rc = run_prepare(ctx, src)) return rc;
-  CK(cudaStreamSynchronize(ctx->stream));  // q_host may be reused on return
+  const int rc = run_prepare(ctx, src);
+  if (staged) stage_release(ctx);
+  if (rc) return rc;
+  return sync_state(ctx);  // q_host may be reused on return; the new dt is read back with it
+}
+
+int fv2d_prefetch_prim(fv2d_ctx *ctx, const double *q_host) {
+  const fv2d::NvtxRange nvtx_range("fv2d_prefetch_prim");
+  if (!ctx || !q_host) return FV2D_ERR_INVALID;
+  if (!mapped_host(q_host)) return fail(ctx, FV2D_ERR_INVALID, "prefetch needs page-locked host memory");
+  const size_t n = (size_t)ctx->p.Nx * ctx->p.Ny * 4;
+  // after the stream's last use of the staging buffer (not after the rest of
+  // its queued work: the copy overlaps a step in flight)
+  CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_stage_free, 0));
+  CK(cudaMemcpyAsync(ctx->stage, q_host, n * sizeof(double), cudaMemcpyHostToDevice, ctx->copy_stream));
+  CK(cudaEventRecord(ctx->ev_prefetch, ctx->copy_stream));
+  ctx->prefetched = q_host;
   return FV2D_OK;
 }
 
@@ -592,8 +651,10 @@ int fv2d_init_problem(fv2d_ctx *ctx, int problem) {
   }
   for (int j = 0; j < p.Ny; ++j)
     for (int i = 0; i < p.Nx; ++i) init_cell(p, problem, i, j, &q[((size_t)j * p.Nx + i) * 4]);
+  stage_take(ctx);
   CK(cudaMemcpyAsync(ctx->stage, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   int rc = run_prepare(ctx, ctx->stage);
+  stage_release(ctx);
   if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));  // q is a local buffer
   return FV2D_OK;
@@ -602,10 +663,12 @@ int fv2d_init_problem(fv2d_ctx *ctx, int problem) {
 static int get_planes(fv2d_ctx *ctx, const double *planes, double *dst, cudaMemcpyKind kind) {
   const fv2d_params &p = ctx->p;
   const long long n = (long long)p.Nx * p.Ny;
+  stage_take(ctx);
   pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(planes, ctx->plane, ctx->pitch, p.Nx, p.Ny,
                                                                      ctx->stage);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(dst, ctx->stage, (size_t)n * 4 * sizeof(double), kind, ctx->stream));
+  stage_release(ctx);
   CK(cudaStreamSynchronize(ctx->stream));
   return FV2D_OK;
 }
@@ -636,7 +699,7 @@ int fv2d_compute_dt(fv2d_ctx *ctx, double *dt, double *inv_hyp, double *inv_tc, 
   const fv2d::NvtxRange nvtx_range("fv2d_compute_dt");
   if (!ctx) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
-  if (int rc = sync_state(ctx)) return rc;
+  if (int rc = fresh_state(ctx)) return rc;
   if (dt) *dt = ctx->st_host->dt;
   if (inv_hyp) *inv_hyp = ctx->st_host->inv_hyp;
   if (inv_tc) *inv_tc = ctx->inv_tc;
@@ -693,6 +756,7 @@ int fv2d_advance(fv2d_ctx *ctx, int max_steps, double tend, double next_save, in
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   if (max_steps < 0) return fail(ctx, FV2D_ERR_INVALID, "max_steps < 0");
   ctx->mirror_valid = false;
+  ctx->st_fresh = false;
   const int check_save = next_save >= 0.0 ? 1 : 0;
   begin_kernel<<<1, 1, 0, ctx->stream>>>(ctx->st, tend, next_save, ctx->p.epsilon, check_save,
                                          skip_first_save_check, max_steps);
@@ -727,6 +791,7 @@ int fv2d_run_async(fv2d_ctx *ctx, int n) {
   if (!ctx || n < 0) return FV2D_ERR_INVALID;
   if (!ctx->have_state) return fail(ctx, FV2D_ERR_STATE, "no state: call set_prim or init_problem first");
   ctx->mirror_valid = false;
+  ctx->st_fresh = false;
   begin_kernel<<<1, 1, 0, ctx->stream>>>(ctx->st, INFINITY, -1.0, ctx->p.epsilon, 0, 1, n);
   CK(cudaGetLastError());
   if (int rc = ensure_graph(ctx)) return rc;

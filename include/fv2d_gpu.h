@@ -71,6 +71,22 @@ int fv2d_init_problem(fv2d_ctx *ctx, int problem);
 int fv2d_set_prim(fv2d_ctx *ctx, const double *q_host);
 int fv2d_get_prim(fv2d_ctx *ctx, double *q_host);
 
+/* Input prefetch (no reference counterpart): starts copying the page-locked
+ * host array q_host (Ny x Nx x 4 doubles) into the context's staging buffer
+ * on a copy stream of its own and returns at once; the state is not changed.
+ * The copy overlaps the work already queued on the context's stream (a step
+ * in flight reads the host link's other direction or not at all), so a
+ * caller that feeds each step a new input from host memory can read the next
+ * input during the current step.  The next fv2d_set_prim(ctx, q_host) with
+ * the same pointer then builds the state from the staging buffer instead of
+ * reading the host link.  q_host must not change between the two calls.  Any
+ * other use of the staging buffer in between (fv2d_set_prim with another
+ * pageable array, fv2d_set_prim_device, fv2d_init_problem, fv2d_get_prim
+ * other than of the host mirror, fv2d_get_cons) waits for the copy and drops
+ * it; fv2d_set_prim then reads q_host again.  FV2D_ERR_INVALID for pageable
+ * memory. */
+int fv2d_prefetch_prim(fv2d_ctx *ctx, const double *q_host);
+
 /* Host mirror (no reference counterpart): registers a page-locked, 16-byte
  * aligned host array of Ny x Nx x 4 doubles that every fv2d_update also
  * writes the new interior primitives into, from the step kernel itself while

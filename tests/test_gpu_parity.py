@@ -378,3 +378,48 @@ def test_page_locked_rounds_match_oracle(gpu_lib):
             assert bits_equal(s.get_cons(), o.get_cons()), c
         s.set_host_mirror(0)
         s.close()
+
+
+def test_prefetched_input_rounds_match_oracle(gpu_lib):
+    """The pipelined end-to-end sequence: the next input prefetched over the
+    host link while the current step runs, then set_prim of that pointer
+    builds the state from the staging buffer -- the oracle's bits, round
+    after round, with a new input each round.  A prefetch dropped by another
+    use of the staging buffer (get_cons, a pageable set_prim) is read again
+    from the host array; pageable memory cannot be prefetched."""
+    torch = pytest.importorskip("torch")
+    from fv2d_gb300 import Fv2dError
+    ny, nx = 37, 50
+    inputs = [random_prim(ny, nx, 30 + k) for k in range(4)]
+    pin_in = torch.zeros((ny, nx, 4), dtype=torch.float64).pin_memory()
+    pin_out = torch.zeros((ny, nx, 4), dtype=torch.float64).pin_memory()
+    for c in G.combo_list()[::23]:
+        p = reference_params(Nx=nx, Ny=ny, gamma0=1.4, CFL=0.6, **c)
+        s, o = gpu_sim(p), Oracle(p)
+        with pytest.raises(Fv2dError):
+            s.prefetch_prim_ptr(inputs[0].ctypes.data)
+        s.set_host_mirror(pin_out.data_ptr())
+        pin_in.numpy()[...] = inputs[0]
+        s.set_prim_ptr(pin_in.data_ptr())
+        for k in range(3):
+            o.set_prim(inputs[k])
+            d = o.compute_dt()
+            assert bits_equal(s.compute_dt()[0], d[0]), c
+            s.update(d[0])
+            o.update(d[0])
+            s.get_prim_ptr(pin_out.data_ptr())
+            assert bits_equal(pin_out.numpy(), o.get_prim()), (c, k)
+            pin_in.numpy()[...] = inputs[k + 1]  # the caller fills the next input, then prefetches it
+            s.prefetch_prim_ptr(pin_in.data_ptr())
+            if k == 1:
+                s.get_cons()  # uses the staging buffer: the prefetch is dropped
+            s.set_prim_ptr(pin_in.data_ptr())
+            o.set_prim(inputs[k + 1])
+            assert bits_equal(s.get_cons(), o.get_cons()), (c, k)
+        # a prefetch followed by a set_prim of another (pageable) array
+        s.prefetch_prim_ptr(pin_in.data_ptr())
+        s.set_prim(inputs[0])
+        s.get_prim_ptr(pin_out.data_ptr())
+        assert bits_equal(pin_out.numpy(), inputs[0]), c
+        s.set_host_mirror(0)
+        s.close()
