@@ -355,28 +355,36 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def fp32_configs(fv):
+def fp32_configs(fv, reduced=False):
     """The two FP32-versus-FP64 benchmark set-ups, each to its end time:
     Kelvin-Helmholtz 4096^2 (CFL 0.7, t = 1) and Rayleigh-Taylor 1024 x 3072
-    with gravity, conduction and viscosity (HLL, t = 5)."""
+    with gravity, conduction and viscosity (HLL, t = 5).  reduced=True: the
+    same set-ups on a quarter of the cells per axis over the first eighth of
+    their end times (KH 1024^2 to t = 0.125, RT 256 x 768 to t = 0.625), small
+    enough for the CPU storage-floor runs of tests/accuracy_floor.py."""
     f = fv.as_float32
+    d = 4 if reduced else 1
+    e = 8.0 if reduced else 1.0
     return {
-        "kh_4096_fp32_vs_fp64": ("kh_step", 1.0, fv.default_params(
-            Nx=4096, Ny=4096, gamma0=f(1.4), CFL=f(0.7), reconstruction=fv.PLM, riemann_solver=fv.HLLC,
+        "kh_%d_fp32_vs_fp64" % (4096 // d): ("kh_step", 1.0 / e, fv.default_params(
+            Nx=4096 // d, Ny=4096 // d, gamma0=f(1.4), CFL=f(0.7), reconstruction=fv.PLM, riemann_solver=fv.HLLC,
             boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC, time_stepping=fv.TS_EULER)),
-        "rt_1024x3072_fp32_vs_fp64": ("rt_hydrostatic", 5.0, fv.default_params(
-            Nx=1024, Ny=3072, xmax=0.5, ymax=1.5, gamma0=f(1.4), CFL=f(0.8), reconstruction=fv.PLM,
+        "rt_%dx%d_fp32_vs_fp64" % (1024 // d, 3072 // d): ("rt_hydrostatic", 5.0 / e, fv.default_params(
+            Nx=1024 // d, Ny=3072 // d, xmax=0.5, ymax=1.5, gamma0=f(1.4), CFL=f(0.8), reconstruction=fv.PLM,
             riemann_solver=fv.HLL, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_REFLECTING,
             time_stepping=fv.TS_EULER, gravity_mode=fv.GRAV_CONSTANT, gy=f(-0.1),
             thermal_conductivity_active=1, kappa=f(1e-4), viscosity_active=1, mu=f(1e-4))),
     }
 
 
-def fp32_vs_fp64(fv, problem, tend, p, device, stream):
+def fp32_vs_fp64(fv, problem, tend, p, device, stream, curve=False):
     """One set-up run to its end time by the plain FP64 path and by the served
     FP32 form from the same initial condition: L1 relative errors of rho and
     p at the end, conservation drift of mass, momentum and energy in both,
-    and the rate of each whole run."""
+    and the rate of each whole run.  curve=True also gives the L1 errors at
+    t = tend k / 8 (the FP64 run stops at each of those times on its way;
+    the service runs the same request to each of them, after the timed
+    run)."""
     import torch
     from fv2d_gb300.serve import Server
     cells = p.Nx * p.Ny
@@ -395,31 +403,48 @@ def fp32_vs_fp64(fv, problem, tend, p, device, stream):
     c0 = sums(sim.get_cons())
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    t64, n64, status = sim.advance(2 ** 31 - 1, tend)
-    e1.record(stream)
-    e1.synchronize()
-    s64 = e0.elapsed_time(e1) * 1e-3
+    marks = [tend * k / 8 for k in range(1, 8)] if curve else []
+    at64 = {}
+    s64, n64 = 0.0, 0
+    for tk in marks + [tend]:
+        e0.record(stream)
+        t64, n, status = sim.advance(2 ** 31 - 1, tk)
+        e1.record(stream)
+        e1.synchronize()
+        s64 += e0.elapsed_time(e1) * 1e-3
+        n64 += n
+        if tk != tend:
+            at64[tk] = (t64, n64, sim.get_prim())
     q64 = sim.get_prim()
     c1 = sums(sim.get_cons())
     sim.close()
-    with Server(budget_bytes=20e9, device=device, autotune=True) as srv:
+    with Server(budget_bytes=40e9, device=device, autotune=True) as srv:
         rid = srv.submit(problem, p, 2 ** 31 - 1, tend=tend)
         if srv.drain(3600) != 0:
             raise RuntimeError("the service did not finish " + problem)
         res = {r.id: r for r in srv.poll()}[rid]
         q32 = srv.get_prim(rid)
+        srv.release(rid)
+        ids = {srv.submit(problem, p, 2 ** 31 - 1, tend=tk): tk for tk in marks}
+        if ids and srv.drain(3600) != 0:
+            raise RuntimeError("the service did not finish " + problem)
+        at32 = {}
+        for r in srv.poll():
+            at32[ids[r.id]] = (r.t, r.steps, srv.get_prim(r.id))
+            srv.release(r.id)
     s32 = res.done_s - res.admit_s
 
-    def l1(k):
-        return float(np.sum(np.abs(q32[..., k] - q64[..., k])) / np.sum(np.abs(q64[..., k])))
+    def l1(a, b, k):
+        return float(np.sum(np.abs(a[..., k] - b[..., k])) / np.sum(np.abs(b[..., k])))
+    points = [{"t_fp64": at64[tk][0], "t_fp32": at32[tk][0], "steps_fp64": at64[tk][1], "steps_fp32": at32[tk][1],
+               "l1_rho": l1(at32[tk][2], at64[tk][2], 0), "l1_p": l1(at32[tk][2], at64[tk][2], 3)} for tk in marks]
     return {"problem": problem, "grid": [p.Nx, p.Ny], "tend": tend,
             "fp64": {"t": t64, "steps": n64, "seconds": s64, "rate": cells * n64 / s64, "unit": METRIC,
                      "drift": drift(c0, c1), "status": status},
             "fp32": {"t": res.t, "steps": res.steps, "seconds": s32, "rate": cells * res.steps / s32, "unit": METRIC,
                      "drift": drift(list(res.cons0), list(res.cons1)), "status": res.status,
                      "timing": "service clock, admission to completion (initial condition, steps, final sums)"},
-            "l1_rho": l1(0), "l1_p": l1(3),
+            "l1_rho": l1(q32, q64, 0), "l1_p": l1(q32, q64, 3), "curve": points,
             "note": "both runs stop at the first t >= tend; their final times differ by less than one dt"}
 
 
@@ -437,6 +462,9 @@ def main():
                     help="skip the FP32-vs-FP64 runs of the Kelvin-Helmholtz 4096^2 and Rayleigh-Taylor 1024x3072 "
                          "set-ups to their end times")
     ap.add_argument("--fp32-configs-only", action="store_true", help="only those two runs")
+    ap.add_argument("--fp32-configs-reduced", action="store_true",
+                    help="with --fp32-configs-only: the reduced set-ups (a quarter of the cells per axis, an eighth of "
+                         "the end time)")
     ap.add_argument("--served-requests", type=int, default=512)
     ap.add_argument("--served-only", action="store_true", help="only the batched FP32 service on the stream")
     ap.add_argument("--served-profile", action="store_true",
@@ -496,8 +524,8 @@ def main():
     if args.fp32_configs_only:
         torch.cuda.set_device(local)
         stream = torch.cuda.Stream()
-        for name, (problem, tend, pc) in fp32_configs(fv).items():
-            print(json.dumps({name: fp32_vs_fp64(fv, problem, tend, pc, local, stream)}), flush=True)
+        for name, (problem, tend, pc) in fp32_configs(fv, args.fp32_configs_reduced).items():
+            print(json.dumps({name: fp32_vs_fp64(fv, problem, tend, pc, local, stream, curve=True)}), flush=True)
         return
     if args.served_profile:
         from fv2d_gb300.serve import Server

@@ -133,9 +133,13 @@ __global__ void __launch_bounds__(256) prepare_kernel(PrepArgs a) {
   const long long n_int = (long long)a.Nx * a.Ny;
   const int W = a.Nx + 4;
   const long long n_ghost = 4LL * W + 4LL * a.Ny;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const Gas<double> gas = make_gas(a.gamma, a.gm1, 1.0 / a.gm1, 0.0);
   double lmax = -1.0;
+  // grid-stride over the interior cells and then the ghost cells: a few
+  // thousand CTAs, so that the reduction's per-CTA atomics on the two state
+  // words stay few
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n_int + n_ghost;
+       idx += (long long)gridDim.x * blockDim.x) {
   if (idx < n_int) {
     const int j = (int)(idx / a.Nx), i = (int)(idx % a.Nx);
     const double *s = a.q_aos + idx * 4;
@@ -177,6 +181,7 @@ __global__ void __launch_bounds__(256) prepare_kernel(PrepArgs a) {
     a.Q[a.plane + g] = nx ? s[1] * -1.0 : s[1];
     a.Q[2 * a.plane + g] = ny ? s[2] * -1.0 : s[2];
     a.Q[3 * a.plane + g] = s[3];
+  }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
@@ -361,7 +366,7 @@ int run_prepare(fv2d_ctx *ctx, const double *src) {
   pa.Nx = p.Nx;
   pa.Ny = p.Ny;
   const long long n = (long long)p.Nx * p.Ny + 4LL * (p.Nx + 4) + 4LL * p.Ny;
-  const int nb = (int)((n + 255) / 256);
+  const int nb = (int)std::min<long long>((n + 255) / 256, 8LL * 152);
   pa.nblocks = nb;
   pa.gamma = ctx->args.gamma;
   pa.gm1 = ctx->args.gm1;

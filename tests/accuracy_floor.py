@@ -13,6 +13,11 @@ that binary32 storage of the state causes by itself, before any binary32
 arithmetic: the floor the service's own error is read against.
 
     python tests/accuracy_floor.py [--every 16] [--nmax 1024] > floor.jsonl
+    python tests/accuracy_floor.py --configs > floor_configs.jsonl
+
+--configs: the reduced Kelvin-Helmholtz and Rayleigh-Taylor set-ups of
+bench.py --fp32-configs-only --fp32-configs-reduced, at t = tend k / 8 (each
+run stops at the first t at or past each of those times).
 """
 import argparse
 import ctypes as C
@@ -69,12 +74,53 @@ def floor_curve(req, points):
     return curve, bg
 
 
+def floor_curve_time(problem, p, tend, n=8):
+    lib = T.oracle_lib()
+    lib.fv2d_oracle_round_cons_f32.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    a = T.Oracle(p)
+    a.init_problem(problem)
+    b = T.Oracle(p)
+    b.init_problem(problem)
+    bg = service_background(b.get_cons(), p.Nx, p.Ny)
+    bgp = bg.ctypes.data_as(C.POINTER(C.c_double))
+    lib.fv2d_oracle_round_cons_f32(b.h, bgp)
+    ta = tb = 0.0
+    na = nb = 0
+    curve = []
+    for k in range(1, n + 1):
+        tk = tend * k / n
+        while ta + p.epsilon < tk:
+            d = a.compute_dt()[0]
+            a.update(d)
+            ta += d
+            na += 1
+        while tb + p.epsilon < tk:
+            d = b.compute_dt()[0]
+            b.update(d)
+            lib.fv2d_oracle_round_cons_f32(b.h, bgp)
+            tb += d
+            nb += 1
+        qa, qb = a.get_prim(), b.get_prim()
+        l1 = [float(np.sum(np.abs(qb[..., f] - qa[..., f])) / np.sum(np.abs(qa[..., f]))) for f in (0, 3)]
+        curve.append({"t": tk, "steps_fp64": na, "steps_floor": nb, "l1_rho": l1[0], "l1_p": l1[1]})
+    return curve
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--every", type=int, default=16)
     ap.add_argument("--nmax", type=int, default=1024)
+    ap.add_argument("--configs", action="store_true")
     args = ap.parse_args()
     import bench
+    if args.configs:
+        import fv2d_gb300 as fv
+        T.oracle_lib().fv2d_oracle_set_threads(os.cpu_count() or 1)
+        for name, (problem, tend, p) in bench.fp32_configs(fv, reduced=True).items():
+            t0 = time.perf_counter()
+            curve = floor_curve_time(problem, p, tend)
+            print(json.dumps({"config": name, "curve": curve, "seconds": time.perf_counter() - t0}), flush=True)
+        return
     from fv2d_gb300.serve import stream_requests
     reqs = stream_requests()
     T.oracle_lib().fv2d_oracle_set_threads(os.cpu_count() or 1)
