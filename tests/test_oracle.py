@@ -249,3 +249,43 @@ def test_openmp_build_of_the_reference_headers_matches_the_oracle():
             o.update(d[0])
             r.update(dr)
         assert bits_equal(o.get_prim(), r.get_prim())
+
+
+def test_round_cons_f32_hook_rounds_the_stored_offsets():
+    """The accuracy-floor hook: every conservative value becomes the binary32
+    rounding of its offset from the background, plus the background; the
+    primitives are rebuilt from it."""
+    import ctypes as C
+    from fv2d_testlib import oracle_lib
+    lib = oracle_lib()
+    lib.fv2d_oracle_round_cons_f32.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    p = reference_params(Nx=24, Ny=16, gamma0=1.4)
+    q = random_prim(16, 24, 3)
+    for bg in (None, np.array([1.3, 0.0, 0.0, 2.7])):
+        o = Oracle(p)
+        o.set_prim(q)
+        u0 = o.get_cons()
+        ptr = None if bg is None else bg.ctypes.data_as(C.POINTER(C.c_double))
+        assert lib.fv2d_oracle_round_cons_f32(o.h, ptr) == 0
+        b = np.zeros(4) if bg is None else bg
+        expect = (u0 - b).astype(np.float32).astype(np.float64) + b
+        assert bits_equal(o.get_cons(), expect)
+        u = o.get_cons()
+        qq = o.get_prim()
+        assert np.allclose(qq[..., 1], u[..., 1] / u[..., 0], rtol=1e-15)
+        assert not bits_equal(o.get_cons(), u0)
+
+
+def test_accuracy_floor_background_matches_the_service_rule():
+    """tests/accuracy_floor.py restates the service's background choice:
+    upper medians of rho and E over the cells (sy/2 + k sy, sx/2 + l sx),
+    sx = max(1, Nx / 64), rounded to binary32."""
+    import accuracy_floor as AF
+    u = np.zeros((100, 130, 4))
+    u[..., 0] = np.arange(100 * 130).reshape(100, 130)
+    u[..., 3] = -u[..., 0]
+    bg = AF.service_background(u, 130, 100)
+    sub = u[0::1, 1::2]  # sy = 1, sx = 2
+    assert bg[0] == float(np.float32(np.sort(sub[..., 0].ravel())[sub[..., 0].size // 2]))
+    assert bg[3] == float(np.float32(np.sort(sub[..., 3].ravel())[sub[..., 3].size // 2]))
+    assert bg[1] == bg[2] == 0.0
