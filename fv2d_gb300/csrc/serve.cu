@@ -442,7 +442,7 @@ int admit(fv2d_server *s, const Pending &pd) {
   batch_cfg_info(cfg, &tx, &ty, &nt, &staging, nullptr, nullptr, nullptr);
   const int items = ((Nx + tx - 1) / tx) * ((Ny + ty - 1) / ty);
   float bg_r = 0.f, bg_e = 0.f;
-  background(r, &bg_r, &bg_e);
+  if (pd.id > 0) background(r, &bg_r, &bg_e);  // the autotuner's synthetic states need none
   // state memory first: a request that does not fit must not grow the work
   // lists (that synchronises the stream and drops the captured graphs)
   void *mem = s->arena.alloc(bytes);
