@@ -183,7 +183,8 @@ def cpu_oracle_rate(n, steps_cap=500, budget_s=12.0):
             "sample": f"sedov {n}x{n}, {steps} iterations after 1 warm-up; {what}", "seconds": el}
 
 
-def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, device=0, active_cells=8e6):
+def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, device=0, active_cells=8e6,
+               single_launch=False):
     """The batched FP32 service on the seeded request stream: requests are
     submitted at their Poisson arrival times; every 16th request is also run
     alone through the plain FP64 path (bit-identical to the reference) for
@@ -191,7 +192,8 @@ def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, de
     from fv2d_gb300.serve import Server, stream_requests, config_name
     reqs = stream_requests(n=n_requests, rate=rate)
     sample = set(range(0, len(reqs), sample_every))
-    srv = Server(budget_bytes=budget, device=device, autotune=True, active_cells=active_cells)
+    srv = Server(budget_bytes=budget, device=device, autotune=True, active_cells=active_cells,
+                 single_launch=single_launch)
     st0 = srv.stats()
     results, ids, keep = {}, {}, {}
     t_start = time.perf_counter()
@@ -476,6 +478,9 @@ def main():
     ap.add_argument("--served-active-cells", type=float, default=8e6,
                     help="service scheduling: shortest remaining work first with about this many cells per step "
                          "(0: every admitted request advances at every step)")
+    ap.add_argument("--served-single-launch", action="store_true",
+                    help="--served-saturated / --served-only: every request in one work list and one launch per "
+                         "step instead of one per grid-size bucket")
     ap.add_argument("--served-tile", default=None,
                     help="kernel configuration for every bucket of the profiling batch (e.g. 28x64/128/march)")
     args = ap.parse_args()
@@ -495,7 +500,8 @@ def main():
         from fv2d_gb300.serve import Server, stream_requests, config_name
         reqs = stream_requests(n=args.served_requests)
         with Server(budget_bytes=150e9, device=local, autotune=args.served_tile is None,
-                    tile_config=args.served_tile, active_cells=args.served_active_cells) as srv:
+                    tile_config=args.served_tile, active_cells=args.served_active_cells,
+                    single_launch=args.served_single_launch) as srv:
             t0 = time.perf_counter()
             for r in reqs:
                 srv.submit(r["problem"], r["params"], r["steps"], lowmach=r["lowmach"])
@@ -511,7 +517,7 @@ def main():
             print(json.dumps({"served_saturated": True, "requests": len(reqs), "cell_updates": work,
                               "wall_s": wall, "rate": work / wall, "unit": METRIC,
                               "p50_s": float(np.median(lat)), "p99_s": float(np.percentile(lat, 99)),
-                              "active_cells": args.served_active_cells,
+                              "active_cells": args.served_active_cells, "single_launch": args.served_single_launch,
                               "tile_configs_per_bucket": [config_name(st.bucket_cfg[b]) for b in range(4)]}),
                   flush=True)
         return
@@ -541,8 +547,9 @@ def main():
     if args.served_only:
         t0 = time.perf_counter()
         served = run_served(fv, n_requests=args.served_requests, device=local,
-                            active_cells=args.served_active_cells)
-        print(json.dumps({"metric": METRIC, "served": served, "wall_s": time.perf_counter() - t0}), flush=True)
+                            active_cells=args.served_active_cells, single_launch=args.served_single_launch)
+        print(json.dumps({"metric": METRIC, "served": served, "wall_s": time.perf_counter() - t0,
+                          "single_launch": args.served_single_launch}), flush=True)
         return
     torch.cuda.set_device(local)
     dist = None

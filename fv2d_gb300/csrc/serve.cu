@@ -396,6 +396,13 @@ size_t state_bytes(const fv2d_params &p, int *pitch, long long *plane, size_t *r
 
 int lane_cfg(const fv2d_server *s, int lane) { return lane < kBuckets ? s->bucket_cfg[lane] : s->ext_cfg; }
 
+// Lane of a request: its grid-size bucket, + kBuckets in the extended
+// family; with single_launch every request of a family shares the family's
+// first lane (one work list, one launch per step).
+int lane_of(const fv2d_server_config &cfg, int bucket, bool ext) {
+  return (cfg.single_launch ? 0 : bucket) + (ext ? kBuckets : 0);
+}
+
 // Grow lane b's work-list buffers to hold `need` items.  New buffers are
 // allocated before the old ones are released, so a failure leaves the lists
 // as they were.
@@ -436,7 +443,7 @@ int admit(fv2d_server *s, const Pending &pd) {
   const size_t bytes = state_bytes(p, &pitch, &plane, &rows_off);
   const int bucket = bucket_of(Nx, Ny);
   const bool ext = needs_ext(p);
-  const int lane = bucket + (ext ? kBuckets : 0);
+  const int lane = lane_of(s->cfg, bucket, ext);
   const int cfg = lane_cfg(s, lane);
   int tx, ty, nt, staging;
   batch_cfg_info(cfg, &tx, &ty, &nt, &staging, nullptr, nullptr, nullptr);
@@ -891,7 +898,7 @@ void fail_all(fv2d_server *s, int code, const std::vector<Pending> &extra) noexc
     r.Nx = p.Nx;
     r.Ny = p.Ny;
     r.bucket = bucket_of(p.Nx, p.Ny);
-    r.lane = r.bucket + (needs_ext(p) ? kBuckets : 0);
+    r.lane = lane_of(s->cfg, r.bucket, needs_ext(p));
     s->n_failed++;
     try {
       s->done_unpolled.push_back(r);
@@ -1063,6 +1070,7 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   if (!cfg || !out || cfg->struct_size != sizeof(fv2d_server_config)) return FV2D_ERR_INVALID;
   if (cfg->max_sims <= 0 || cfg->max_sims > 16384 || !(cfg->budget_bytes > 0)) return FV2D_ERR_INVALID;
   if (!(cfg->active_cells >= 0) || std::isinf(cfg->active_cells)) return FV2D_ERR_INVALID;
+  if (cfg->single_launch != 0 && cfg->single_launch != 1) return FV2D_ERR_INVALID;
   *out = nullptr;
   fv2d_server *s = new (std::nothrow) fv2d_server();
   if (!s) return FV2D_ERR_NOMEM;
@@ -1123,6 +1131,8 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   } else if (cfg->autotune) {
     autotune(s);
   }
+  if (cfg->single_launch)  // one configuration for the merged list: the largest grids'
+    for (int b = 0; b < kBuckets - 1; ++b) s->bucket_cfg[b] = s->bucket_cfg[kBuckets - 1];
   if (s->ext_cfg < 0) {  // no extended configuration can run on this device
     fv2d_server_destroy(s);
     return FV2D_ERR_CUDA;

@@ -64,6 +64,11 @@ typedef struct fv2d_server_config {
                                work first -- the requests with the fewest remaining cell-updates advance,
                                about this many cells per step (at least one request); the others stay
                                resident in HBM until they rank among them */
+  int32_t single_launch;    /* 0: one work list and one launch per lane (grid-size bucket x kernel family), the
+                               lanes as parallel graph branches.  1: every request of a kernel family in one
+                               work list, advanced by one persistent launch per step with one configuration
+                               (the one chosen for the largest grids) */
+  int32_t pad;
 } fv2d_server_config;
 
 typedef struct fv2d_request {

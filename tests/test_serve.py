@@ -127,6 +127,31 @@ def k_ext(p):
             or (p.thermal_conductivity_active and (p.thermal_conductivity_mode != 0 or p.bctc_ymin or p.bctc_ymax)))
 
 
+def test_single_launch_form_same_alone_and_in_the_mix(gpu_lib):
+    """single_launch: every request of a kernel family in one work list and
+    one persistent launch per step; a request's result is still the same
+    alone and in the mix, bit for bit."""
+    from fv2d_gb300.serve import Server
+    reqs = mixed_requests()
+    alone = []
+    with Server(budget_bytes=4e9, autotune=False, single_launch=True) as s:
+        for pb, p, n, lm in reqs:
+            rid = s.submit(pb, p, n, lowmach=lm)
+            assert s.drain(120) == 0
+            res = {r.id: r for r in s.poll()}
+            assert res[rid].status == 0 and res[rid].steps == n
+            assert res[rid].lane in (0, 4)
+            alone.append(s.get_prim(rid))
+    with Server(budget_bytes=4e9, autotune=False, single_launch=True, active_cells=3e5) as s:
+        fillers = [s.submit("sedov", params(N), 30 + N // 16) for N in (64, 320, 512, 192, 96)]
+        ids = [s.submit(pb, p, n, lowmach=lm) for pb, p, n, lm in reqs]
+        assert s.drain(120) == 0
+        res = {r.id: r for r in s.poll()}
+        assert all(res[i].status == 0 for i in ids + fillers)
+        for k, rid in enumerate(ids):
+            assert bits_equal(s.get_prim(rid), alone[k]), reqs[k][0]
+
+
 def l1_rel(a, b):
     return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
 
