@@ -471,6 +471,9 @@ def main():
     ap.add_argument("--served-only", action="store_true", help="only the batched FP32 service on the stream")
     ap.add_argument("--served-profile", action="store_true",
                     help="fixed batch for kernel profiling: 12 Sedov 768^2 requests x 60 steps")
+    ap.add_argument("--served-profile-steps", type=int, default=60,
+                    help="--served-profile: steps per request (profile a launch well after the first replays, "
+                         "when every request of the batch is resident)")
     ap.add_argument("--served-saturated", action="store_true",
                     help="service rate without arrival gaps: the request stream submitted at once")
     ap.add_argument("--served-accuracy", action="store_true",
@@ -481,8 +484,11 @@ def main():
     ap.add_argument("--served-single-launch", action="store_true",
                     help="--served-saturated / --served-only: every request in one work list and one launch per "
                          "step instead of one per grid-size bucket")
+    ap.add_argument("--served-band", type=int, default=0,
+                    help="--served-saturated / --served-profile: rows per work item of the march kernels (0: chosen "
+                         "per lane)")
     ap.add_argument("--served-tile", default=None,
-                    help="kernel configuration for every bucket of the profiling batch (e.g. 28x64/128/march)")
+                    help="kernel configuration for every bucket of the profiling batch (e.g. 28/32x20/march)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -500,7 +506,7 @@ def main():
         from fv2d_gb300.serve import Server, stream_requests, config_name
         reqs = stream_requests(n=args.served_requests)
         with Server(budget_bytes=150e9, device=local, autotune=args.served_tile is None,
-                    tile_config=args.served_tile, active_cells=args.served_active_cells,
+                    tile_config=args.served_tile, active_cells=args.served_active_cells, band_rows=args.served_band,
                     single_launch=args.served_single_launch) as srv:
             t0 = time.perf_counter()
             for r in reqs:
@@ -535,10 +541,11 @@ def main():
         return
     if args.served_profile:
         from fv2d_gb300.serve import Server
-        with Server(budget_bytes=20e9, device=local, autotune=False, tile_config=args.served_tile) as srv:
+        with Server(budget_bytes=20e9, device=local, autotune=False, tile_config=args.served_tile,
+                    band_rows=args.served_band) as srv:
             p = workload_params(fv, 768)
             for _ in range(12):
-                srv.submit("sedov", p, 60)
+                srv.submit("sedov", p, args.served_profile_steps)
             srv.drain(300)
             st = srv.stats()
             print(json.dumps({"served_profile": True, "completed": st.completed, "cell_updates": st.cell_updates,

@@ -48,6 +48,7 @@ UNITS = [
     ("selftest.cu", ["-fmad=false"]),
     ("noalloc.cu", ["-fmad=false"]),
     ("batch_kernels.cu", ["-use_fast_math"]),
+    ("batch_march2.cu", ["-use_fast_math"]),
     ("serve.cu", []),
     ("problems.cpp", []),
     ("../host/ini.cpp", []),

@@ -15,6 +15,12 @@ enum { SIM_FREE = 0, SIM_ACTIVE = 1, SIM_DONE = 2, SIM_FAILED = 3 };
 // Reconstructions of the served step (the values of fv2d_params.reconstruction
 // they come from: PCM and PCM_WB -> PCM, PLM, MUSCL_HANCOCK).
 enum { BR_PCM = 0, BR_PLM = 2, BR_MH = 3 };
+// Kernel families of the served step (bit f of a configuration's family
+// mask: it runs requests of family f): plain hydro (HLL / HLLC, PCM / PLM,
+// constant gravity), diffusive (the same with constant conduction and / or
+// viscosity), extended (FSLP, MUSCL-Hancock, per-row tables, boundary
+// fluxes).
+enum { FAM_PLAIN = 0, FAM_DIFF = 1, FAM_EXT = 2, kFamilies = 3 };
 // Gravity and conductivity forms of the served step.
 enum { BG_NONE = 0, BG_CONST = 1, BG_ROW = 2 };  // BG_ROW: per-row table (analytical gravity)
 enum { BK_NONE = 0, BK_CONST = 1, BK_ROW = 2 };  // BK_ROW: per-row face conductivities (B02)
@@ -39,6 +45,7 @@ struct __align__(64) SimDev {
   int pitch;            // floats per padded row
   int Nx, Ny;           // interior cells
   int ntx, nty;         // work items along x and y (for the kernel configuration of its lane)
+  int band;             // rows per work item: the tile height, or the march kernels' band (chosen per lane)
   int cur;              // buffer holding the current state
   int status;           // SIM_*
   int step, max_steps;  // committed steps, stop after max_steps
@@ -107,7 +114,9 @@ struct BatchArgs {
 
 // Polls of the second, final wait for a tile copy that outlived ctl[1].
 constexpr unsigned int kTileWaitFinal = 1u << 24;
-enum { BATCH_ERR_TMA_TIMEOUT = 1 };
+// BATCH_ERR_FAMILY: a request reached a kernel built without its family's
+// terms (the service's lanes keep that from happening).
+enum { BATCH_ERR_TMA_TIMEOUT = 1, BATCH_ERR_FAMILY = 2 };
 
 // Source and destination buffers of the stage a launch runs: Euler and the
 // first SSP-RK2 stage read the current buffer and write the other one; the

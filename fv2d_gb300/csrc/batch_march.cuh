@@ -149,7 +149,7 @@ __device__ __forceinline__ S4<float> yflux(const S4<float> &top, const S4<float>
 
 // One work item (see the header comment), with the Riemann solver, the
 // reconstruction and the family fixed at compile time.
-template <int H, int RS, int RECON, bool EXT>
+template <int RS, int RECON, bool EXT>
 __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem item, const bm::WarpSim &W,
                                            const int lane) {
   using namespace bm;
@@ -210,7 +210,8 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
   const int gxl = item.tx * STRIP + lane;           // padded column of this lane
   const bool colok = gxl < Nx + 4;
   const bool out_lane = lane >= 2 && lane < 30 && gxl - 2 < Nx;
-  const int j0 = item.ty * H, jend = min(j0 + H, Ny);  // interior rows [j0, jend)
+  const int band = FV2D_SIM(W, band);
+  const int j0 = item.ty * band, jend = min(j0 + band, Ny);  // interior rows [j0, jend)
   const float dtdx = S.dt * S.inv_dx, dtdy = S.dt * S.inv_dy;
   const float ax = 0.5f * S.dt * S.inv_dx, ay = 0.5f * S.dt * S.inv_dy;  // MUSCL-Hancock half step
 
@@ -474,7 +475,7 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
 }
 
 // The common family: HLL / HLLC x PCM / PLM.
-template <int H, int NT, int MINB>
+template <int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a) {
   const int lane = threadIdx.x & 31;
   const int nwarps = gridDim.x * (NT / 32);
@@ -488,34 +489,34 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a
     const bool plm = FV2D_SIM(W, recon) == BR_PLM;
     if (FV2D_SIM(W, rs) == RS_HLL) {
       if (plm)
-        march_item<H, RS_HLL, BR_PLM, false>(a, item, W, lane);
+        march_item<RS_HLL, BR_PLM, false>(a, item, W, lane);
       else
-        march_item<H, RS_HLL, BR_PCM, false>(a, item, W, lane);
+        march_item<RS_HLL, BR_PCM, false>(a, item, W, lane);
     } else {
       if (plm)
-        march_item<H, RS_HLLC, BR_PLM, false>(a, item, W, lane);
+        march_item<RS_HLLC, BR_PLM, false>(a, item, W, lane);
       else
-        march_item<H, RS_HLLC, BR_PCM, false>(a, item, W, lane);
+        march_item<RS_HLLC, BR_PCM, false>(a, item, W, lane);
     }
     __syncwarp();
   }
 }
 
-template <int H, int RS>
+template <int RS>
 __device__ __forceinline__ void march_ext_recon(const BatchArgs &a, const WorkItem item, const bm::WarpSim &W,
                                                 const int lane) {
   const int recon = FV2D_SIM(W, recon);
   if (recon == BR_MH)
-    march_item<H, RS, BR_MH, true>(a, item, W, lane);
+    march_item<RS, BR_MH, true>(a, item, W, lane);
   else if (recon == BR_PLM)
-    march_item<H, RS, BR_PLM, true>(a, item, W, lane);
+    march_item<RS, BR_PLM, true>(a, item, W, lane);
   else
-    march_item<H, RS, BR_PCM, true>(a, item, W, lane);
+    march_item<RS, BR_PCM, true>(a, item, W, lane);
 }
 
 // The extended family: HLL / HLLC / FSLP x PCM / PLM / MUSCL-Hancock, with
 // the per-row tables and the boundary fluxes.
-template <int H, int NT, int MINB>
+template <int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_march_ext_kernel(const BatchArgs a) {
   const int lane = threadIdx.x & 31;
   const int nwarps = gridDim.x * (NT / 32);
@@ -526,11 +527,11 @@ __global__ void __launch_bounds__(NT, MINB) batch_march_ext_kernel(const BatchAr
     if (FV2D_SIM(W, status) != SIM_ACTIVE) continue;
     const int rs = FV2D_SIM(W, rs);
     if (rs == RS_HLL)
-      march_ext_recon<H, RS_HLL>(a, item, W, lane);
+      march_ext_recon<RS_HLL>(a, item, W, lane);
     else if (rs == RS_FSLP)
-      march_ext_recon<H, RS_FSLP>(a, item, W, lane);
+      march_ext_recon<RS_FSLP>(a, item, W, lane);
     else
-      march_ext_recon<H, RS_HLLC>(a, item, W, lane);
+      march_ext_recon<RS_HLLC>(a, item, W, lane);
     __syncwarp();
   }
 }

@@ -52,13 +52,18 @@ namespace {
 
 constexpr int kBuckets = 4;
 // Work lists, kernel launches and graph branches are per lane: a grid-size
-// bucket of one kernel family (lanes 0-3 the common family, 4-7 the extended
-// one).
-constexpr int kLanes = 2 * kBuckets;
-constexpr int kMaxCfgs = 32;  // capacity of the per-configuration tables (batch_kernels.cu asserts the bound)
-int num_cfgs() { return std::min(batch_num_cfgs(), kMaxCfgs); }
+// bucket of one kernel family (lanes 0-3 the plain family, 4-7 the diffusive
+// one, 8-11 the extended one).
+constexpr int kLanes = kFamilies * kBuckets;
+int num_cfgs() { return batch_num_cfgs(); }
 constexpr int kConsBlocks = 64;
 constexpr int kMinSide = 16, kMaxSide = 8192;  // accepted Nx, Ny
+// Band heights the march lanes choose from (rows per work item), tallest
+// first, and the work items per resident warp a lane's launch should have.
+constexpr int kBands[] = {32, 24, 16, 12, 8};
+constexpr int kMinBand = 8;
+constexpr double kItemsPerWarp = 1.5;
+static_assert(offsetof(SimDev, band) == offsetof(SimDev, nty) + sizeof(int), "nty and band are updated by one copy");
 
 // Grid-size bucket of an Nx x Ny grid, by its cell count (the side of the
 // square with as many cells: < 128, < 256, < 512, larger).
@@ -66,10 +71,11 @@ int bucket_of(int Nx, int Ny) {
   const double c = (double)Nx * Ny;
   return c < 128.0 * 128 ? 0 : (c < 256.0 * 256 ? 1 : (c < 512.0 * 512 ? 2 : 3));
 }
-int cfg_ext(int c) {
-  int e = 0;
-  batch_cfg_info(c, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &e);
-  return e;
+// kernel families configuration c runs (bit FAM_*)
+int cfg_fams(int c) {
+  int f = 0;
+  batch_cfg_info(c, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &f);
+  return f;
 }
 
 // ---------------------------------------------------------------- kernels
@@ -226,6 +232,7 @@ struct Slot {
   int64_t id = -1;
   fv2d_request req;
   int bucket = 0, lane = 0, cfg = 0;
+  int items = 0;  // work-list entries reserved for it (its items at the smallest band height)
   void *mem = nullptr;
   size_t bytes = 0;
   double submit_s = 0, admit_s = 0;
@@ -255,15 +262,15 @@ struct fv2d_server {
   CUtensorMap *d_tmaps = nullptr, *h_tmaps = nullptr;
   std::vector<Slot> slots;
   std::vector<int> free_slots;
-  // per-lane work lists (lane = bucket, + kBuckets for the extended family)
+  // per-lane work lists (lane = bucket + kBuckets * family)
   WorkItem *d_work[kLanes] = {};
   int *d_nwork = nullptr, *h_nwork = nullptr;
   WorkItem *h_work[kLanes] = {};
   int work_cap[kLanes] = {};
   int items_in[kLanes] = {};  // work items of the resident requests, per lane
-  int bucket_cfg[kBuckets] = {1, 2, 3, 3};  // common-family configuration per bucket
-  int ext_cfg = -1;                         // extended-family configuration (every bucket)
-  int cfg_grid[kMaxCfgs] = {};
+  // configuration per family and bucket (the extended family: one for every bucket)
+  int fam_cfg[kFamilies][kBuckets] = {{1, 2, 3, 3}, {1, 2, 3, 3}, {-1, -1, -1, -1}};
+  std::vector<int> cfg_grid;  // persistent grid per configuration (0: cannot run here)
   bool lists_dirty = true;
   int mask = 0;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (K, lane mask) -> graph
@@ -336,14 +343,20 @@ const char *check_request(const fv2d_request &r) {
   return nullptr;
 }
 
-// The kernel family a request needs: the extended one for FSLP, the
-// MUSCL-Hancock predictor, analytical gravity, B02 conductivity, the
-// y-boundary conduction modes and the well-balanced y flux.
+// The extended family serves FSLP, the MUSCL-Hancock predictor, analytical
+// gravity, B02 conductivity, the y-boundary conduction modes and the
+// well-balanced y flux.
 bool needs_ext(const fv2d_params &p) {
   return p.riemann_solver == FV2D_FSLP || p.reconstruction == FV2D_MUSCL_HANCOCK ||
          p.gravity_mode == FV2D_GRAV_ANALYTICAL || p.well_balanced_flux_at_y_bc ||
          (p.thermal_conductivity_active && (p.thermal_conductivity_mode != FV2D_TCM_CONSTANT ||
                                             p.bctc_ymin != FV2D_BCTC_NONE || p.bctc_ymax != FV2D_BCTC_NONE));
+}
+// The kernel family of a request: extended, else diffusive (constant
+// conduction or viscosity), else plain.
+int family_of(const fv2d_params &p) {
+  if (needs_ext(p)) return FAM_EXT;
+  return (p.thermal_conductivity_active || p.viscosity_active) ? FAM_DIFF : FAM_PLAIN;
 }
 bool needs_rows(const fv2d_params &p) {
   return p.gravity_mode == FV2D_GRAV_ANALYTICAL ||
@@ -394,13 +407,13 @@ size_t state_bytes(const fv2d_params &p, int *pitch, long long *plane, size_t *r
   return needs_rows(p) ? *rows_off + sizeof(float) * kRowStride * (size_t)p.Ny : planes;
 }
 
-int lane_cfg(const fv2d_server *s, int lane) { return lane < kBuckets ? s->bucket_cfg[lane] : s->ext_cfg; }
+int lane_cfg(const fv2d_server *s, int lane) { return s->fam_cfg[lane / kBuckets][lane % kBuckets]; }
 
-// Lane of a request: its grid-size bucket, + kBuckets in the extended
-// family; with single_launch every request of a family shares the family's
-// first lane (one work list, one launch per step).
-int lane_of(const fv2d_server_config &cfg, int bucket, bool ext) {
-  return (cfg.single_launch ? 0 : bucket) + (ext ? kBuckets : 0);
+// Lane of a request: its grid-size bucket + kBuckets * its family; with
+// single_launch every request of a family shares the family's first lane
+// (one work list, one launch per step).
+int lane_of(const fv2d_server_config &cfg, int bucket, int family) {
+  return (cfg.single_launch ? 0 : bucket) + family * kBuckets;
 }
 
 // Grow lane b's work-list buffers to hold `need` items.  New buffers are
@@ -442,12 +455,15 @@ int admit(fv2d_server *s, const Pending &pd) {
   size_t rows_off;
   const size_t bytes = state_bytes(p, &pitch, &plane, &rows_off);
   const int bucket = bucket_of(Nx, Ny);
-  const bool ext = needs_ext(p);
-  const int lane = lane_of(s->cfg, bucket, ext);
+  const int family = family_of(p);
+  const bool ext = family == FAM_EXT;
+  const int lane = lane_of(s->cfg, bucket, family);
   const int cfg = lane_cfg(s, lane);
   int tx, ty, nt, staging;
   batch_cfg_info(cfg, &tx, &ty, &nt, &staging, nullptr, nullptr, nullptr);
-  const int items = ((Nx + tx - 1) / tx) * ((Ny + ty - 1) / ty);
+  // the march kernels' band height changes with the lane's contents: room for
+  // the most items it can take
+  const int items = ((Nx + tx - 1) / tx) * ((Ny + (staging == 2 ? kMinBand : ty) - 1) / (staging == 2 ? kMinBand : ty));
   float bg_r = 0.f, bg_e = 0.f;
   if (pd.id > 0) background(r, &bg_r, &bg_e);  // the autotuner's synthetic states need none
   // state memory first: a request that does not fit must not grow the work
@@ -468,6 +484,7 @@ int admit(fv2d_server *s, const Pending &pd) {
   sl.bucket = bucket;
   sl.lane = lane;
   sl.cfg = cfg;
+  sl.items = items;
   sl.mem = mem;
   sl.bytes = bytes;
   sl.submit_s = pd.submit_s;
@@ -485,6 +502,7 @@ int admit(fv2d_server *s, const Pending &pd) {
   d.Nx = Nx;
   d.Ny = Ny;
   d.ntx = (Nx + tx - 1) / tx;
+  d.band = ty;  // the march lanes' band is set by rebuild_lists
   d.nty = (Ny + ty - 1) / ty;
   d.cur = 0;
   d.status = SIM_ACTIVE;
@@ -623,6 +641,32 @@ double remaining_work(const fv2d_server *s, int slot) {
   return std::max(steps, 1.0) * cells;
 }
 
+// Band height of a march lane for the simulations it is about to run: the
+// tallest of kBands that gives the launch at least kItemsPerWarp work items
+// per resident warp, else the shortest.  Measured on single grids (one
+// simulation in the lane; KH 4096^2 and RT 1024 x 3072, bands 12..64): the
+// rate falls by 10-20 % when the items end within one or a little over one
+// wave of the resident warps (the last warps run alone, or every warp runs
+// its one item in step with the others), while the extra window fill of a
+// shorter band costs a few per cent; bands taller than 32 rows gained
+// nothing where the items were plentiful and lost 9 % at 64.  A
+// simulation's results do not depend on the band: every face is computed by
+// the same code whichever band holds it.
+int choose_band(const fv2d_server *s, int lane, const std::vector<int> &slots) {
+  const int c = lane_cfg(s, lane);
+  int tx, ty, nt, staging;
+  batch_cfg_info(c, &tx, &ty, &nt, &staging, nullptr, nullptr, nullptr);
+  if (staging != 2 || slots.empty()) return ty;  // tile kernels: the tile height
+  if (s->cfg.band_rows > 0) return s->cfg.band_rows;
+  const double warps = (double)s->cfg_grid[c] * (nt / 32);
+  for (int H : kBands) {
+    double items = 0;
+    for (int k : slots) items += (double)s->h_up[k].ntx * ((s->h_up[k].Ny + H - 1) / H);
+    if (items >= kItemsPerWarp * warps) return H;
+  }
+  return kMinBand;
+}
+
 void rebuild_lists(fv2d_server *s) {
   std::vector<WorkItem> lists[kLanes];
   // shortest remaining work first, up to about active_cells cells per step
@@ -645,6 +689,15 @@ void rebuild_lists(fv2d_server *s) {
   }
   s->mask = 0;
   for (int b = 0; b < kLanes; ++b) {
+    const int band = choose_band(s, b, per_lane[b]);
+    for (int slot : per_lane[b]) {
+      SimDev &u = s->h_up[slot];
+      if (u.band != band) {  // nty and band, adjacent in the table entry
+        u.band = band;
+        u.nty = (u.Ny + band - 1) / band;
+        cudaMemcpyAsync(&s->d_sims[slot].nty, &u.nty, 2 * sizeof(int), cudaMemcpyHostToDevice, s->stream);
+      }
+    }
     for (int slot : per_lane[b]) {
       const SimDev &d = s->h_up[slot];
       for (int ty = 0; ty < d.nty; ++ty)
@@ -792,7 +845,7 @@ void retire_all(fv2d_server *s, const std::vector<int> &done) {
     fin.bg_e = d.bg_e;
     r.done_s = t_done;
     s->arena.release(sl.mem, sl.bytes);
-    s->items_in[sl.lane] -= d.ntx * d.nty;
+    s->items_in[sl.lane] -= sl.items;
     s->n_active--;
     sl.used = false;
     sl.mem = nullptr;
@@ -898,7 +951,7 @@ void fail_all(fv2d_server *s, int code, const std::vector<Pending> &extra) noexc
     r.Nx = p.Nx;
     r.Ny = p.Ny;
     r.bucket = bucket_of(p.Nx, p.Ny);
-    r.lane = lane_of(s->cfg, r.bucket, needs_ext(p));
+    r.lane = lane_of(s->cfg, r.bucket, family_of(p));
     s->n_failed++;
     try {
       s->done_unpolled.push_back(r);
@@ -988,10 +1041,11 @@ void worker_main(fv2d_server *s) {
 }
 
 // One autotuner trial: nsims synthetic Sedov requests of Nx x Ny (PLM +
-// HLLC) stepped with the bucket's current configuration; returns the rate in
+// HLLC; with constant conduction and viscosity for the diffusive family)
+// stepped with the bucket's current configuration; returns the rate in
 // cell-updates/s, or -1 when the trial could not run.  Leaves the server
 // empty.
-double autotune_trial(fv2d_server *s, int Nx, int Ny, int nsims) {
+double autotune_trial(fv2d_server *s, int family, int Nx, int Ny, int nsims) {
   for (int k = 0; k < nsims; ++k) {
     Pending pd;
     pd.id = -1 - k;
@@ -1004,6 +1058,12 @@ double autotune_trial(fv2d_server *s, int Nx, int Ny, int nsims) {
     pd.req.params.gamma0 = 1.4;
     pd.req.params.reconstruction = FV2D_PLM;
     pd.req.params.riemann_solver = FV2D_HLLC;
+    if (family == FAM_DIFF) {
+      pd.req.params.thermal_conductivity_active = 1;
+      pd.req.params.kappa = 1e-4;
+      pd.req.params.viscosity_active = 1;
+      pd.req.params.mu = 1e-4;
+    }
     pd.req.max_steps = 1 << 30;
     pd.req.tend = 0;
     pd.submit_s = 0;
@@ -1037,36 +1097,55 @@ double autotune_trial(fv2d_server *s, int Nx, int Ny, int nsims) {
   return ok ? cells * steps / (ms * 1e-3) : -1.0;
 }
 
-// Per bucket, the common-family configuration with the best measured rate.
-// Buckets 0-2 are scored on a batch of square grids of their representative
-// side.  The largest bucket holds both many mid-size grids and single grids of
-// millions of cells, which favour different band heights (many grids: taller
-// bands, less halo work; one grid: shorter bands, enough work items to fill
-// the resident warps several times over), so it is scored by the geometric
-// mean of two trials: 40 grids of 768^2 and one grid of 1024 x 3072 (the
-// first alone when the HBM budget cannot hold the second).
+// Per family (plain, diffusive), the configuration that runs a mixture of
+// requests in the least time, used for every bucket of the family.  The
+// mixture holds one request per bucket (sides 96, 192, 384, 768: as many
+// requests of each size, like sides spread log-uniformly, so that the cells
+// and the time are mostly the large grids'); each bucket's rate is measured
+// on a batch of about 24e6 cells of its size, and the largest bucket's as the
+// geometric mean of that batch and one grid of 1024 x 3072 (the batch alone
+// when the HBM budget cannot hold the grid), since it also holds single grids
+// of millions of cells, which favour other work-item shapes.  One
+// configuration per family: lanes that ran different kernels side by side
+// (parallel graph branches) measured slower on the request stream than either
+// kernel alone, and per-bucket choices from short trials changed from one
+// start to the next.  The trials run under the service's own scheduling cap
+// (active_cells), so a configuration is judged at the load its lanes will
+// carry: on the 512-request stream at 8e6 cells per step the one-column march
+// (smaller work items, more resident warps) gave p50 0.089 s against 0.103 s
+// for the two-column one, which wins on full lanes (the same stream submitted
+// at once: 50.1 against 48.9 G cell-updates/s).
 void autotune(fv2d_server *s) {
   const int rep[kBuckets] = {96, 192, 384, 768};
   const int ncfg = num_cfgs();
-  for (int b = 0; b < kBuckets; ++b) {
-    const int N = rep[b];
-    const int nsims = std::max(2, std::min(256, (int)(24e6 / ((double)N * N))));
+  for (int f : {FAM_PLAIN, FAM_DIFF}) {
     double best = -1;
-    int best_cfg = s->bucket_cfg[b];
+    int best_cfg = s->fam_cfg[f][kBuckets - 1];
     for (int c = 0; c < ncfg; ++c) {
-      if (!s->cfg_grid[c] || cfg_ext(c)) continue;  // the common family's configurations
-      s->bucket_cfg[b] = c;
-      double score = autotune_trial(s, N, N, nsims);
-      if (b == kBuckets - 1 && score > 0) {
-        const double single = autotune_trial(s, 1024, 3072, 1);  // -1 when the budget cannot hold it
-        if (single > 0) score = std::sqrt(score * single);
+      if (!s->cfg_grid[c] || !((cfg_fams(c) >> f) & 1)) continue;  // the family's configurations
+      for (int b = 0; b < kBuckets; ++b) s->fam_cfg[f][b] = c;
+      double cells = 0, time = 0;  // one request of each bucket
+      bool ok = true;
+      for (int b = 0; b < kBuckets && ok; ++b) {
+        const int N = rep[b];
+        const int nsims = std::max(2, std::min(256, (int)(24e6 / ((double)N * N))));
+        double r = autotune_trial(s, f, N, N, nsims);
+        if (b == kBuckets - 1 && r > 0) {
+          const double single = autotune_trial(s, f, 1024, 3072, 1);  // -1 when the budget cannot hold it
+          if (single > 0) r = std::sqrt(r * single);
+        }
+        ok = r > 0;
+        cells += (double)N * N;
+        time += ok ? (double)N * N / r : 0.0;
       }
+      if (!ok) continue;
+      const double score = cells / time;
       if (score > best) {
         best = score;
         best_cfg = c;
       }
     }
-    s->bucket_cfg[b] = best_cfg;
+    for (int b = 0; b < kBuckets; ++b) s->fam_cfg[f][b] = best_cfg;
   }
   cudaStreamSynchronize(s->stream);
   s->free_slots.clear();
@@ -1089,6 +1168,7 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   if (cfg->max_sims <= 0 || cfg->max_sims > 16384 || !(cfg->budget_bytes > 0)) return FV2D_ERR_INVALID;
   if (!(cfg->active_cells >= 0) || std::isinf(cfg->active_cells)) return FV2D_ERR_INVALID;
   if (cfg->single_launch != 0 && cfg->single_launch != 1) return FV2D_ERR_INVALID;
+  if (cfg->band_rows != 0 && (cfg->band_rows < kMinBand || cfg->band_rows > 64)) return FV2D_ERR_INVALID;
   *out = nullptr;
   fv2d_server *s = new (std::nothrow) fv2d_server();
   if (!s) return FV2D_ERR_NOMEM;
@@ -1133,25 +1213,29 @@ int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   cudaMemcpy(s->d_nwork, s->h_nwork, sizeof(int) * kLanes, cudaMemcpyHostToDevice);
   s->slots.resize(s->max_sims);
   for (int k = s->max_sims - 1; k >= 0; --k) s->free_slots.push_back(k);
+  s->cfg_grid.assign(num_cfgs(), 0);
   for (int c = 0; c < num_cfgs(); ++c) {
     int per_sm = 0;
     if (batch_setup(c, &per_sm) == cudaSuccess && per_sm > 0) s->cfg_grid[c] = per_sm * s->num_sms;
   }
   // the extended family: its first configuration that can run
-  for (int c = 0; c < num_cfgs() && s->ext_cfg < 0; ++c)
-    if (cfg_ext(c) && s->cfg_grid[c]) s->ext_cfg = c;
+  for (int c = 0; c < num_cfgs() && s->fam_cfg[FAM_EXT][0] < 0; ++c)
+    if (((cfg_fams(c) >> FAM_EXT) & 1) && s->cfg_grid[c])
+      for (int b = 0; b < kBuckets; ++b) s->fam_cfg[FAM_EXT][b] = c;
+  // a forced configuration serves the families it has item bodies for; the
+  // others keep their defaults
   const int forced = cfg->tile_config - 1;
   if (forced >= 0 && forced < num_cfgs() && s->cfg_grid[forced]) {
-    if (cfg_ext(forced))
-      s->ext_cfg = forced;
-    else
-      for (int b = 0; b < kBuckets; ++b) s->bucket_cfg[b] = forced;
+    for (int f = 0; f < kFamilies; ++f)
+      if ((cfg_fams(forced) >> f) & 1)
+        for (int b = 0; b < kBuckets; ++b) s->fam_cfg[f][b] = forced;
   } else if (cfg->autotune) {
     autotune(s);
   }
-  if (cfg->single_launch)  // one configuration for the merged list: the largest grids'
-    for (int b = 0; b < kBuckets - 1; ++b) s->bucket_cfg[b] = s->bucket_cfg[kBuckets - 1];
-  if (s->ext_cfg < 0) {  // no extended configuration can run on this device
+  if (cfg->single_launch)  // one configuration for a family's merged list: its largest grids'
+    for (int f = 0; f < kFamilies; ++f)
+      for (int b = 0; b < kBuckets - 1; ++b) s->fam_cfg[f][b] = s->fam_cfg[f][kBuckets - 1];
+  if (s->fam_cfg[FAM_EXT][0] < 0) {  // no extended configuration can run on this device
     fv2d_server_destroy(s);
     return FV2D_ERR_CUDA;
   }
@@ -1313,8 +1397,11 @@ int fv2d_server_get_stats(fv2d_server *s, fv2d_server_stats *out) {
   out->busy_s = s->pub.busy_s;
   out->bytes_in_use = s->pub.bytes_in_use;
   out->bytes_reserved = s->pub.bytes_reserved;
-  for (int b = 0; b < kBuckets; ++b) out->bucket_cfg[b] = s->bucket_cfg[b];
-  out->ext_cfg = s->ext_cfg;
+  for (int b = 0; b < kBuckets; ++b) {
+    out->bucket_cfg[b] = s->fam_cfg[FAM_PLAIN][b];
+    out->diff_cfg[b] = s->fam_cfg[FAM_DIFF][b];
+  }
+  out->ext_cfg = s->fam_cfg[FAM_EXT][0];
   out->replays = s->pub.replays;
   return FV2D_OK;
 }

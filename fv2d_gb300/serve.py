@@ -13,7 +13,7 @@ class ServerConfig(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("device", C.c_int32), ("budget_bytes", C.c_double),
                 ("max_sims", C.c_int32), ("autotune", C.c_int32), ("steps_per_replay", C.c_int32),
                 ("tile_config", C.c_int32), ("active_cells", C.c_double), ("single_launch", C.c_int32),
-                ("pad", C.c_int32)]
+                ("band_rows", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -39,7 +39,7 @@ class Stats(C.Structure):
                 ("failed", C.c_int64), ("active", C.c_int32), ("queued", C.c_int32),
                 ("cell_updates", C.c_double), ("busy_s", C.c_double), ("bytes_in_use", C.c_double),
                 ("bytes_reserved", C.c_double), ("bucket_cfg", C.c_int32 * 4), ("replays", C.c_int32),
-                ("ext_cfg", C.c_int32)]
+                ("ext_cfg", C.c_int32), ("diff_cfg", C.c_int32 * 4)]
 
 
 def _bind(L):
@@ -91,14 +91,16 @@ class Server:
     """A running batched service on one GPU."""
 
     def __init__(self, budget_bytes=150e9, device=0, max_sims=4096, autotune=True, steps_per_replay=0,
-                 tile_config=None, active_cells=0.0, single_launch=False):
+                 tile_config=None, active_cells=0.0, single_launch=False, band_rows=0):
         """tile_config: name of a kernel configuration (config_name) to use for
         every grid-size bucket instead of the defaults or the autotuner.
         active_cells: 0 advances every admitted request at every step; a
         positive value schedules shortest remaining work first, about that
         many cells per step.
         single_launch: every request of a kernel family in one work list and
-        one persistent launch per step (instead of one per grid-size bucket)."""
+        one persistent launch per step (instead of one per grid-size bucket).
+        band_rows: rows per work item of the march kernels (0: chosen per
+        lane to fill whole waves of resident warps)."""
         self.L = _bind(_lib_loader())
         forced = 0
         if tile_config is not None:
@@ -107,7 +109,7 @@ class Server:
                 raise ValueError(f"unknown tile configuration {tile_config!r}; known: {names}")
             forced = names.index(tile_config) + 1
         cfg = ServerConfig(C.sizeof(ServerConfig), device, float(budget_bytes), max_sims, 1 if autotune else 0,
-                           steps_per_replay, forced, float(active_cells), 1 if single_launch else 0, 0)
+                           steps_per_replay, forced, float(active_cells), 1 if single_launch else 0, int(band_rows))
         self.h = C.c_void_p()
         rc = self.L.fv2d_server_create(C.byref(cfg), C.byref(self.h))
         if rc != 0:

@@ -19,13 +19,19 @@
  *     requests (first in, first out, smaller ones may pass a request that
  *     does not fit) while the HBM budget and the simulation table allow;
  *   - every admitted state stays resident in HBM until it completes;
+ *   - requests fall into three kernel families: plain (HLL / HLLC, PCM /
+ *     PLM, constant gravity), diffusive (the same with constant conduction
+ *     and / or viscosity) and extended (FSLP, MUSCL-Hancock, analytical
+ *     gravity, B02 conductivity, the y-boundary conduction modes, the
+ *     well-balanced y flux);
  *   - all admitted simulations advance together: per lane (grid-size bucket
  *     of one kernel family) one persistent kernel launch per stage walks a
  *     (simulation, tile) work list, each simulation reduces its own dt; an
  *     SSP-RK2 step takes two launches; a CUDA graph replays several launches
  *     between admissions and retirements, the lanes as parallel branches;
- *   - tile shape, threads per tile and halo staging are chosen per bucket by
- *     an autotuner at start-up (or fixed defaults).
+ *   - the kernel configuration (tile shape or column strip, threads per
+ *     CTA, halo staging) is chosen per family by an autotuner at start-up,
+ *     one for all of the family's buckets (or fixed defaults per bucket).
  * A simulation's result does not depend on what else was in the batch.
  *
  * Failures:
@@ -57,9 +63,10 @@ typedef struct fv2d_server_config {
   int32_t device;           /* CUDA device */
   double budget_bytes;      /* HBM budget for simulation states (admission control) */
   int32_t max_sims;         /* simulation table capacity (<= 16384) */
-  int32_t autotune;         /* 1: time the tile configurations per bucket at start-up */
+  int32_t autotune;         /* 1: time the kernel configurations per family at start-up */
   int32_t steps_per_replay; /* 0: adaptive (about 3 ms of work per graph replay) */
-  int32_t tile_config;      /* 0: defaults or autotuned; k > 0: configuration k - 1 for every bucket */
+  int32_t tile_config;      /* 0: defaults or autotuned; k > 0: configuration k - 1 for every bucket of the
+                               kernel families it serves (the others keep their defaults) */
   double active_cells;      /* 0: every admitted request advances at every step.  > 0: shortest remaining
                                work first -- the requests with the fewest remaining cell-updates advance,
                                about this many cells per step (at least one request); the others stay
@@ -68,7 +75,8 @@ typedef struct fv2d_server_config {
                                lanes as parallel graph branches.  1: every request of a kernel family in one
                                work list, advanced by one persistent launch per step with one configuration
                                (the one chosen for the largest grids) */
-  int32_t pad;
+  int32_t band_rows;        /* 0: the march kernels' rows per work item are chosen per lane at every work-list
+                               rebuild (to fill whole waves of the launch's resident warps); 8..64: that many */
 } fv2d_server_config;
 
 typedef struct fv2d_request {
@@ -92,7 +100,7 @@ typedef struct fv2d_result {
   uint64_t negatives;/* cells reset by the negative density/pressure guard */
   int32_t Nx, Ny;
   int32_t bucket;    /* grid-size bucket (0..3) */
-  int32_t lane;      /* bucket, + 4 when the extended kernel family ran it */
+  int32_t lane;      /* bucket, + 4 when the diffusive kernel family ran it, + 8 for the extended one */
 } fv2d_result;
 
 typedef struct fv2d_server_stats {
@@ -102,9 +110,10 @@ typedef struct fv2d_server_stats {
   double busy_s;         /* wall time with at least one active simulation */
   double bytes_in_use;   /* HBM held by resident states */
   double bytes_reserved; /* HBM reserved by the state arena */
-  int32_t bucket_cfg[4]; /* common-family configuration index per bucket (see fv2d_server_config_name) */
+  int32_t bucket_cfg[4]; /* plain-family configuration index per bucket (see fv2d_server_config_name) */
   int32_t replays;       /* graph replays launched */
   int32_t ext_cfg;       /* extended-family configuration index */
+  int32_t diff_cfg[4];   /* diffusive-family configuration index per bucket */
 } fv2d_server_stats;
 
 int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out);

@@ -67,7 +67,7 @@ def _params(N, **kw):
     return fv.default_params(**base)
 
 
-@pytest.mark.parametrize("tile", [None, "28x64/128/march"])
+@pytest.mark.parametrize("tile", [None, "28/128x4/march"])
 def test_served_nan_request_fails_alone(gpu_lib, tile):
     import fv2d_gb300 as fv
     from fv2d_gb300.serve import Server

@@ -85,8 +85,9 @@ def mixed_requests():
     ]
 
 
-# the default tile kernel and the register-resident column-marching kernel
-TILES = [None, "28x64/128/march", "28x32/64/march"]
+# the default tile kernel and the register-resident column-marching kernels (one and two columns per lane; a
+# two-column configuration serves one family, the others keep their defaults)
+TILES = [None, "28/128x4/march", "28/64x8/march", "60/32x16/march2", "60/32x10/march2-diff"]
 
 
 @pytest.mark.parametrize("active", [0.0, 3e5])
@@ -104,7 +105,7 @@ def test_same_result_alone_and_in_the_mix(gpu_lib, tile, active):
             res = {r.id: r for r in s.poll()}
             assert res[rid].status == 0 and res[rid].steps == n
             assert (res[rid].Nx, res[rid].Ny) == (p.Nx, p.Ny)
-            assert res[rid].lane >= 4 if k_ext(p) else res[rid].lane < 4
+            assert res[rid].lane // 4 == k_family(p) and res[rid].lane % 4 == res[rid].bucket
             alone.append((s.get_prim(rid), res[rid].t))
     with Server(budget_bytes=4e9, autotune=False, tile_config=tile, active_cells=active) as s:
         fillers = [s.submit("sedov", params(N), 30 + N // 16) for N in (64, 320, 512, 192, 96)]
@@ -119,12 +120,15 @@ def test_same_result_alone_and_in_the_mix(gpu_lib, tile, active):
             assert bits_equal(s.get_prim(rid), q), reqs[k][0]
 
 
-def k_ext(p):
-    """Whether a request runs in the extended kernel family."""
+def k_family(p):
+    """The kernel family a request runs in: 2 extended, 1 diffusive (constant
+    conduction or viscosity), 0 plain."""
     import fv2d_gb300 as fv
-    return (p.riemann_solver == fv.FSLP or p.reconstruction == fv.MUSCL_HANCOCK
+    if (p.riemann_solver == fv.FSLP or p.reconstruction == fv.MUSCL_HANCOCK
             or p.gravity_mode == fv.GRAV_ANALYTICAL or p.well_balanced_flux_at_y_bc
-            or (p.thermal_conductivity_active and (p.thermal_conductivity_mode != 0 or p.bctc_ymin or p.bctc_ymax)))
+            or (p.thermal_conductivity_active and (p.thermal_conductivity_mode != 0 or p.bctc_ymin or p.bctc_ymax))):
+        return 2
+    return 1 if (p.thermal_conductivity_active or p.viscosity_active) else 0
 
 
 def test_single_launch_form_same_alone_and_in_the_mix(gpu_lib):
@@ -140,7 +144,7 @@ def test_single_launch_form_same_alone_and_in_the_mix(gpu_lib):
             assert s.drain(120) == 0
             res = {r.id: r for r in s.poll()}
             assert res[rid].status == 0 and res[rid].steps == n
-            assert res[rid].lane in (0, 4)
+            assert res[rid].lane == 4 * k_family(p)
             alone.append(s.get_prim(rid))
     with Server(budget_bytes=4e9, autotune=False, single_launch=True, active_cells=3e5) as s:
         fillers = [s.submit("sedov", params(N), 30 + N // 16) for N in (64, 320, 512, 192, 96)]
