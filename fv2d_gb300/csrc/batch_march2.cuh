@@ -272,38 +272,59 @@ __device__ __forceinline__ void march2_item(const BatchArgs &a, const WorkItem i
   };
   const f2 hp5 = F2(0.5f), hm5 = F2(-0.5f);
 
-  // The row loop of batch_march.cuh: iteration L loads padded row L; the
-  // first four iterations fill the window, the others update row C = L - 2;
-  // every row and every y face enters through this one code path.
-  // The window carries only what cannot be re-derived cheaply: the
-  // primitives of rows C and C + 1, the y slope of row C, the y flux of face
-  // C - 1/2 and the prefetched next row.  The difference q(C+1) - q(C) is
-  // formed again, the conservative row C is read again (an L1 hit: it was
-  // loaded two iterations earlier) and the primitives of row C - 1 are
-  // rebuilt from memory only when conduction or viscosity need them.  Every
-  // operation here is an explicit packed intrinsic or an exact instruction,
-  // so a value formed again is bit-identical to the first one.
+  // The row loop of batch_march.cuh, with its four window-fill iterations
+  // peeled into a prologue so that the main loop's y-face and x-face solves,
+  // which are independent, share one block the compiler can interleave.
+  // Iteration L loads padded row L and (from L = j0 + 4 on) updates row
+  // C = L - 2.  Both copies of the row entry and of the y face are the same
+  // functions of the same operands, and every operation in them is an explicit
+  // packed intrinsic or an exact instruction (nothing is left for the compiler
+  // to contract), so a face that two bands share gets bit-identical fluxes from
+  // the prologue of one and the main loop of the other: the step stays exactly
+  // conservative.
+  // The window carries the primitives of rows L - 2 and L - 1 (q0, qp), the
+  // y slope of row L - 2, the y flux of face C - 1/2 and the prefetched next
+  // row; the conservative row C is read again at its update (an L1 hit: it
+  // was loaded two iterations earlier) and the primitives of row C - 1 are
+  // rebuilt from memory only when conduction or viscosity need them.
   Q2 q0 = z, qp = z, h0 = z, Gm = z;
+  f2 Unext[4];
   float lmax = 0.f;
   unsigned nneg = 0, nnan = 0;
-  f2 Unext[4];
+  // primitives of the new row L and the y slope of row L - 1
+  auto enter = [&](const f2 Un[4], Q2 &qn, Q2 &hp) {
+    qn = to_prim(Un, S);
+    hp = yslope(ydiff(q0, qp), ydiff(qp, qn));
+  };
+  // y face between rows L - 2 and L - 1
+  auto yface = [&](const Q2 &hp) {
+    f2 pout;
+    return swap_uv(solve<RS>(swap_uv(face(q0, h0, hp5)), swap_uv(face(qp, hp, hm5)), gas, pout));
+  };
   load(j0, Unext);
-  for (int L = j0; L < jend + 4; ++L) {
+  for (int L = j0; L < j0 + 4; ++L) {  // jend >= j0 + 1: row L + 1 is in the band's window
+    const f2 Un[4] = {Unext[0], Unext[1], Unext[2], Unext[3]};
+    load(L + 1, Unext);
+    Q2 qn, hp;
+    enter(Un, qn, hp);
+    if (L == j0 + 3) Gm = yface(hp);
+    q0 = qp;
+    qp = qn;
+    h0 = hp;
+  }
+  for (int L = j0 + 4; L < jend + 4; ++L) {
     const int C = L - 2;
     const int j = C - 2;
-    f2 Un[4] = {Unext[0], Unext[1], Unext[2], Unext[3]};
+    const f2 Un[4] = {Unext[0], Unext[1], Unext[2], Unext[3]};
     if (L + 1 < jend + 4) load(L + 1, Unext);
-    const Q2 qn = to_prim(Un, S);
-    const Q2 Dn = ydiff(qp, qn);
-    const Q2 hp = yslope(ydiff(q0, qp), Dn);  // slope of row L - 1
-    f2 poutP = F2(0.f);
-    Q2 Gp = z;
-    if (L >= j0 + 3)  // face between rows C and C + 1
-      Gp = swap_uv(solve<RS>(swap_uv(face(q0, h0, hp5)), swap_uv(face(qp, hp, hm5)), gas, poutP));
-    if (L >= j0 + 4) {
+    Q2 qn, hp;
+    enter(Un, qn, hp);
+    const Q2 Gp = yface(hp);  // face between rows C and C + 1
+    {
       // x faces of row C: the pair solves faces 2l - 1/2 and 2l + 1/2
       const Q2 hx = xslope(q0);
-      const Q2 Fw = solve<RS>(left(face(q0, hx, hp5)), face(q0, hx, hm5), gas, poutP);
+      f2 poutX;
+      const Q2 Fw = solve<RS>(left(face(q0, hx, hp5)), face(q0, hx, hm5), gas, poutX);
       const Q2 Fe = right(Fw);
 
       // update in the reference's order: x flux, x gravity, y flux, y
@@ -461,7 +482,7 @@ __device__ __forceinline__ void march2_item(const BatchArgs &a, const WorkItem i
           }
         }
       }
-    }  // L >= j0 + 4
+    }
 
     // advance the window
     q0 = qp;
