@@ -102,13 +102,14 @@ def test_server_config_layout_matches_header(libs):
 
 
 def test_server_rejects_bad_configs_without_gpu(libs):
-    """Checked before any CUDA call: size, table capacity, budget, scheduling cap, launch form."""
+    """Checked before any CUDA call: size, table capacity, budget, scheduling cap, launch form, band height."""
     from fv2d_gb300.serve import ServerConfig, _bind
     lib = _bind(libs)
     good = dict(device=0, budget_bytes=1e9, max_sims=16, autotune=0, steps_per_replay=0, tile_config=0,
                 active_cells=0.0)
     for bad in (dict(max_sims=0), dict(max_sims=1 << 20), dict(budget_bytes=0.0), dict(active_cells=-1.0),
-                dict(active_cells=float("nan")), dict(active_cells=float("inf")), dict(single_launch=2)):
+                dict(active_cells=float("nan")), dict(active_cells=float("inf")), dict(single_launch=2),
+                dict(band_rows=-1), dict(band_rows=4), dict(band_rows=65)):
         kw = dict(good, **bad)
         cfg = ServerConfig(C.sizeof(ServerConfig), **kw)
         h = C.c_void_p()

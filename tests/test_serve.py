@@ -156,6 +156,28 @@ def test_single_launch_form_same_alone_and_in_the_mix(gpu_lib):
             assert bits_equal(s.get_prim(rid), alone[k]), reqs[k][0]
 
 
+@pytest.mark.parametrize("tile", ["28/32x20/march", "60/32x16/march2", "60/32x10/march2-diff"])
+def test_band_height_does_not_change_results(gpu_lib, tile):
+    """The march kernels' rows per work item (chosen per lane, or fixed by
+    band_rows) change only how the grid is cut into work items: every face is
+    computed by the same code whichever band holds it, so the results are the
+    same bits for any band, including bands that do not divide Ny."""
+    from fv2d_gb300.serve import Server
+    reqs = mixed_requests()
+    runs = []
+    for band in (0, 8, 13, 64):
+        with Server(budget_bytes=4e9, autotune=False, tile_config=tile, band_rows=band) as s:
+            ids = [s.submit(pb, p, n, lowmach=lm) for pb, p, n, lm in reqs]
+            assert s.drain(120) == 0
+            res = {r.id: r for r in s.poll()}
+            assert all(res[i].status == 0 for i in ids)
+            runs.append([(s.get_prim(i), res[i].t) for i in ids])
+    for other in runs[1:]:
+        for k, ((q, t), (q0, t0)) in enumerate(zip(other, runs[0])):
+            assert t == t0, reqs[k][0]
+            assert bits_equal(q, q0), reqs[k][0]
+
+
 def l1_rel(a, b):
     return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
 
