@@ -83,14 +83,19 @@ struct __align__(64) SimDev {
 // loses two or more bits).  Elsewhere the binary32 evaluation is within a
 // unit or two of the binary64 one rounded to binary32, so the binary64 pipe
 // (1/64 of the FP32 rate) is not used.
+// Every operation is an explicitly rounded intrinsic, which the compiler
+// never contracts into a multiply-add: each inlined copy of this function
+// gives the same bits for the same operands (kernels that evaluate a row in
+// two code paths rely on that).
 __device__ __forceinline__ float pressure_of(float dE, float bg_e, float r, float u, float v, float gm1,
                                              int lowmach) {
-  const float ek = 0.5f * r * (u * u + v * v);
-  if (lowmach && fabsf(ek) > 0.25f * fabsf(dE + bg_e)) {
+  const float ek = __fmul_rn(__fmul_rn(0.5f, r), __fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)));
+  if (lowmach && fabsf(ek) > __fmul_rn(0.25f, fabsf(__fadd_rn(dE, bg_e)))) {
     const double rd = r, ud = u, vd = v;
-    return (float)((((double)dE - 0.5 * rd * (ud * ud + vd * vd)) + (double)bg_e) * (double)gm1);
+    const double ekd = __dmul_rn(__dmul_rn(0.5, rd), __dadd_rn(__dmul_rn(ud, ud), __dmul_rn(vd, vd)));
+    return (float)__dmul_rn(__dadd_rn(__dsub_rn((double)dE, ekd), (double)bg_e), (double)gm1);
   }
-  return ((dE - ek) + bg_e) * gm1;
+  return __fmul_rn(__fadd_rn(__fsub_rn(dE, ek), bg_e), gm1);
 }
 
 __device__ __forceinline__ bool is_nan_f(float x) { return (__float_as_uint(x) & 0x7FFFFFFFu) > 0x7F800000u; }

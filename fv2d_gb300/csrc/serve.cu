@@ -62,7 +62,7 @@ constexpr int kMinSide = 16, kMaxSide = 8192;  // accepted Nx, Ny
 // first, and the work items per resident warp a lane's launch should have.
 constexpr int kBands[] = {32, 24, 16, 12, 8};
 constexpr int kMinBand = 8;
-constexpr double kItemsPerWarp = 1.5;
+constexpr double kItemsPerWarp = 2.0;
 static_assert(offsetof(SimDev, band) == offsetof(SimDev, nty) + sizeof(int), "nty and band are updated by one copy");
 
 // Grid-size bucket of an Nx x Ny grid, by its cell count (the side of the
@@ -644,12 +644,13 @@ double remaining_work(const fv2d_server *s, int slot) {
 // Band height of a march lane for the simulations it is about to run: the
 // tallest of kBands that gives the launch at least kItemsPerWarp work items
 // per resident warp, else the shortest.  Measured on single grids (one
-// simulation in the lane; KH 4096^2 and RT 1024 x 3072, bands 12..64): the
-// rate falls by 10-20 % when the items end within one or a little over one
-// wave of the resident warps (the last warps run alone, or every warp runs
-// its one item in step with the others), while the extra window fill of a
-// shorter band costs a few per cent; bands taller than 32 rows gained
-// nothing where the items were plentiful and lost 9 % at 64.  A
+// simulation in the lane; KH 4096^2 and RT 1024 x 3072, bands 12..64) and on
+// batches of 12 and 40 Sedov 768^2 grids: the rate falls by 10-20 % when the
+// items end within one or a little over one wave of the resident warps (the
+// last warps run alone, or every warp runs its one item in step with the
+// others), by a few per cent still at 1.5 items per warp, while the extra
+// window fill of a shorter band costs a few per cent; bands taller than 32
+// rows gained nothing where the items were plentiful and lost 9 % at 64.  A
 // simulation's results do not depend on the band: every face is computed by
 // the same code whichever band holds it.
 int choose_band(const fv2d_server *s, int lane, const std::vector<int> &slots) {
