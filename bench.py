@@ -285,7 +285,7 @@ def served_accuracy(fv, sample_every=16, device=0):
     on what else is in the batch, so the runs to different step counts share
     one batch) and the FP64 path advances through the same checkpoints.  L1
     errors are sum |a - b| / sum |b| over the interior."""
-    from fv2d_gb300.serve import Server, stream_requests
+    from fv2d_gb300.serve import Server, stream_requests, config_name
     reqs = stream_requests()
     sub = list(range(0, len(reqs), sample_every))
     pts = {i: checkpoints(reqs[i]["steps"]) for i in sub}
@@ -293,6 +293,9 @@ def served_accuracy(fv, sample_every=16, device=0):
     res = {}
     # the kernel configurations the service runs in production (autotuned)
     with Server(budget_bytes=100e9, device=device, autotune=True) as srv:
+        st = srv.stats()
+        chosen = {"plain": config_name(st.bucket_cfg[0]), "diffusive": config_name(st.diff_cfg[0]),
+                  "extended": config_name(st.ext_cfg)}
         ids = {}
         for i in sub:
             for n in pts[i]:
@@ -331,7 +334,7 @@ def served_accuracy(fv, sample_every=16, device=0):
                "median_l1_rho": float(np.median([w["l1_rho"] for w in rows])),
                "median_l1_p": float(np.median([w["l1_p"] for w in rows])),
                "l1_rho_le_1e-5": sum(w["l1_rho"] <= 1e-5 for w in rows),
-               "mass_drift_max": max(w.get("mass_drift", 0.0) for w in rows)}
+               "mass_drift_max": max(w.get("mass_drift", 0.0) for w in rows), "kernel_configurations": chosen}
     return rows, summary
 
 
