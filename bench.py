@@ -18,9 +18,11 @@ device from the previous state.
           also writes the new state into a registered page-locked host
           mirror while it computes), fv2d_get_prim on that mirror.
 
-`--impl reference` times the reference algorithm on the host cores: the
-CPU oracle (an OpenMP restatement of the reference's pass structure, bit-exact
-with the reference's headers), on the same workload.
+`--impl reference` times the reference's own step code on the host cores (its
+headers built with OpenMP over rows in place of Kokkos' dispatch, from the
+sources staged into baseline/_ref), on the same workload; where those sources
+are not staged, the CPU oracle (an OpenMP restatement of the reference's pass
+structure, bit-exact with the reference's headers) stands in.
 
 Launched as `python bench.py --gpus N --steps K --warmup W` (N = 1) or under
 torch.distributed.run for N > 1: ranks run independent replicas (the step

@@ -1,23 +1,25 @@
-// batch_march2.cuh -- the common family of the served FP32 step with two
-// columns per lane and packed binary32 arithmetic.
+// batch_march2.cuh -- the plain and diffusive families of the served FP32
+// step with two columns per lane and packed binary32 arithmetic.
 //
 // Same work decomposition as batch_march.cuh, but a warp owns a strip of 64
 // padded columns (60 interior columns plus the 2-column halo on each side) and
 // lane l holds columns 2l and 2l + 1 as the two halves of float2 registers.
 // Both columns run the same instructions, so every binary32 add, multiply and
 // multiply-add of the step is issued once for the pair (sm_100 packed
-// FADD2 / FMUL2 / FFMA2, which the item body is bound by: issue, not the FMA
-// pipe); selects, comparisons, min / max, reciprocals and square roots stay
-// per column.  The pair also halves the warp shuffles per cell (a column's
-// left or right neighbour is in the same lane half the time), the 64-bit loads
-// and stores halve the memory instructions, and the halo is 4 of 64 columns
-// instead of 4 of 32.
+// FADD2 / FMUL2 / FFMA2: the one-column body is bound by instruction issue,
+// not by the FMA pipe); selects, comparisons, min / max, reciprocals and
+// square roots stay per column.  The pair also halves the warp shuffles per
+// cell (a column's left or right neighbour is in the same lane half the
+// time), the 64-bit loads and stores halve the memory instructions, and the
+// halo is 4 of 64 columns instead of 4 of 32.
 //
 // Physics and update order are those of the one-column kernel (States.h:32-43,
 // RiemannSolvers.h:7-128, Update.h:93-174 with constant gravity,
 // ThermalConduction.h:36-73 with constant conductivity, Viscosity.h:27-119):
-// HLL or HLLC, PCM or PLM.  Each face is solved once, by one code path, so the
-// step stays exactly conservative across lanes, strips and bands.
+// HLL or HLLC, PCM or PLM.  Each face is solved once; a face that two bands
+// share is solved by both, in code whose every operation is an explicitly
+// rounded intrinsic or an exact instruction, so both get the same bits and
+// the step stays exactly conservative across lanes, strips and bands.
 #pragma once
 
 #include "batch_march.cuh"

@@ -1111,7 +1111,7 @@ double autotune_trial(fv2d_server *s, int family, int Nx, int Ny, int nsims) {
 // (parallel graph branches) measured slower on the request stream than either
 // kernel alone, and per-bucket choices from short trials changed from one
 // start to the next.  The trials run under the service's own scheduling cap
-// (active_cells), so a configuration is judged at the load its lanes will
+// (active_cells), so a configuration is measured at the load its lanes will
 // carry: on the 512-request stream at 8e6 cells per step the one-column march
 // (smaller work items, more resident warps) gave p50 0.089 s against 0.103 s
 // for the two-column one, which wins on full lanes (the same stream submitted
