@@ -2,7 +2,8 @@
 //
 // One warp owns a work item: a strip of 32 padded columns (28 interior
 // columns plus a 2-column halo on each side) of one simulation, over a band
-// of H rows.  Lane l holds column i0 + l and marches down the band: each new
+// of rows (its height is the simulation's `band`, which the service sets per
+// lane).  Lane l holds column i0 + l and marches down the band: each new
 // row is loaded once (coalesced), converted to primitives and kept in a
 // 4-row register window; x neighbours come from warp shuffles, y neighbours
 // from the window.  Every face is solved once (x faces in the lane on their
@@ -12,11 +13,11 @@
 // Update.h:93-174, ThermalConduction.h:36-108, Viscosity.h:27-119), and the
 // same per-simulation commit of the step (ComputeDt.h:64, main.cpp:62-83).
 //
-// Two families of item bodies, each compiled per Riemann solver and
+// Two kernels of item bodies, each compiled per Riemann solver and
 // reconstruction so that the row loop carries neither branch:
-//   - the common one (batch_march_kernel): HLL or HLLC, PCM or PLM, constant
-//     gravity, constant conductivity, viscosity;
-//   - the extended one (batch_march_ext_kernel): also FSLP and the
+//   - batch_march_kernel, for the plain and the diffusive families: HLL or
+//     HLLC, PCM or PLM, constant gravity, constant conductivity, viscosity;
+//   - batch_march_ext_kernel, for the extended family: also FSLP and the
 //     MUSCL-Hancock predictor, gravity and conductivity from per-row tables
 //     (analytical gravity, B02 conductivity), the y-boundary conduction
 //     modes and the well-balanced y-boundary flux.
@@ -474,7 +475,7 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
   }
 }
 
-// The common family: HLL / HLLC x PCM / PLM.
+// The plain and diffusive families: HLL / HLLC x PCM / PLM.
 template <int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_march_kernel(const BatchArgs a) {
   const int lane = threadIdx.x & 31;

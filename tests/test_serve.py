@@ -73,7 +73,7 @@ def mixed_requests():
         ("gresho_vortex", params(64, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC,
                                  gresho_Mach=fv.as_float32(0.05)), 100, True),
         ("rt_hydrostatic", rt_rect(), 40, False),
-        # SSP-RK2 in the common family, rectangular
+        # SSP-RK2 in the plain family, rectangular
         ("kh_step", params(128, Ny=96, boundary_x=fv.BC_PERIODIC, boundary_y=fv.BC_PERIODIC, seed=3,
                            time_stepping=fv.TS_RK2), 30, False),
         # the extended family
