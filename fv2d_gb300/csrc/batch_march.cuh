@@ -45,19 +45,33 @@ __device__ __forceinline__ S4<float> shfl_down4(const S4<float> &q, int d) {
 __device__ __forceinline__ S4<float> add4(const S4<float> &a, const S4<float> &b) {
   return S4<float>{a.r + b.r, a.u + b.u, a.v + b.v, a.p + b.p};
 }
+// Component-wise operations on the state's two halves (rho, u) and (v, p) as
+// packed binary32 pairs (sm_100 FADD2 / FMUL2 / FFMA2): one issue per pair,
+// the same single rounding per component as the scalar forms.
+__device__ __forceinline__ float2 lo2(const S4<float> &a) { return make_float2(a.r, a.u); }
+__device__ __forceinline__ float2 hi2(const S4<float> &a) { return make_float2(a.v, a.p); }
+__device__ __forceinline__ S4<float> join4(float2 lo, float2 hi) { return S4<float>{lo.x, lo.y, hi.x, hi.y}; }
 __device__ __forceinline__ S4<float> sub4(const S4<float> &a, const S4<float> &b) {
-  return S4<float>{a.r - b.r, a.u - b.u, a.v - b.v, a.p - b.p};
+  const float2 m1 = make_float2(-1.f, -1.f);
+  return join4(__ffma2_rn(lo2(b), m1, lo2(a)), __ffma2_rn(hi2(b), m1, hi2(a)));
 }
 // minmod slope from the differences to the left and right neighbours
 // (Update.h:59-91); each difference is formed once and serves the slopes of
 // both cells it separates
+__device__ __forceinline__ float minmod_p(float dl, float dr, float prod) {
+  const float m = fabsf(dl) < fabsf(dr) ? dl : dr;
+  return prod < 0.f ? 0.f : m;
+}
 __device__ __forceinline__ S4<float> slope4(const S4<float> &dl, const S4<float> &dr) {
-  return S4<float>{minmod(dl.r, dr.r), minmod(dl.u, dr.u), minmod(dl.v, dr.v), minmod(dl.p, dr.p)};
+  const float2 pl = __fmul2_rn(lo2(dl), lo2(dr)), ph = __fmul2_rn(hi2(dl), hi2(dr));
+  return S4<float>{minmod_p(dl.r, dr.r, pl.x), minmod_p(dl.u, dr.u, pl.y), minmod_p(dl.v, dr.v, ph.x),
+                   minmod_p(dl.p, dr.p, ph.y)};
 }
 // reconstructed face state q + slope * sign * 0.5 (Update.h:25), one
 // multiply-add per field
 __device__ __forceinline__ S4<float> face4(const S4<float> &q, const S4<float> &s, float half) {
-  return S4<float>{fmaf(half, s.r, q.r), fmaf(half, s.u, q.u), fmaf(half, s.v, q.v), fmaf(half, s.p, q.p)};
+  const float2 h = make_float2(half, half);
+  return join4(__ffma2_rn(h, lo2(s), lo2(q)), __ffma2_rn(h, hi2(s), hi2(q)));
 }
 __device__ __forceinline__ S4<float> swap_uv(const S4<float> &q) { return S4<float>{q.r, q.v, q.u, q.p}; }
 
@@ -309,19 +323,25 @@ __device__ __forceinline__ void march_item(const BatchArgs &a, const WorkItem it
 
       // update in the reference's order: x flux, x gravity, y flux, y gravity,
       // conduction, viscosity (Update.h:114-168, 176-191)
-      float un[4] = {U0[0], U0[1], U0[2], U0[3]};
-      un[0] += (Fw.r - Fe.r) * dtdx;
-      un[1] += (Fw.u - Fe.u) * dtdx;
-      un[2] += (Fw.v - Fe.v) * dtdx;
-      un[3] += (Fw.p - Fe.p) * dtdx;
+      float un[4];
+      {
+        const float2 d = make_float2(dtdx, dtdx);
+        const S4<float> dF = sub4(Fw, Fe);
+        const float2 lo = __ffma2_rn(lo2(dF), d, make_float2(U0[0], U0[1]));
+        const float2 hi = __ffma2_rn(hi2(dF), d, make_float2(U0[2], U0[3]));
+        un[0] = lo.x; un[1] = lo.y; un[2] = hi.x; un[3] = hi.y;
+      }
       if (S.grav) {
         un[2] += S.dt * q0.r * g_x;
         un[3] += S.dt * 0.5f * (Fw.r + Fe.r) * g_x;
       }
-      un[0] += (GmU.r - GpU.r) * dtdy;
-      un[1] += (GmU.u - GpU.u) * dtdy;
-      un[2] += (GmU.v - GpU.v) * dtdy;
-      un[3] += (GmU.p - GpU.p) * dtdy;
+      {
+        const float2 d = make_float2(dtdy, dtdy);
+        const S4<float> dG = sub4(GmU, GpU);
+        const float2 lo = __ffma2_rn(lo2(dG), d, make_float2(un[0], un[1]));
+        const float2 hi = __ffma2_rn(hi2(dG), d, make_float2(un[2], un[3]));
+        un[0] = lo.x; un[1] = lo.y; un[2] = hi.x; un[3] = hi.y;
+      }
       if (S.grav) {
         un[2] += S.dt * q0.r * g_y;
         un[3] += S.dt * 0.5f * (GmU.r + GpU.r) * g_y;
