@@ -1164,6 +1164,11 @@ const char *fv2d_server_config_name(int index) {
   return name;
 }
 
+int fv2d_server_config_families(int index) {
+  if (index < 0 || index >= batch_num_cfgs()) return -1;
+  return cfg_fams(index);
+}
+
 int fv2d_server_create(const fv2d_server_config *cfg, fv2d_server **out) {
   if (!cfg || !out || cfg->struct_size != sizeof(fv2d_server_config)) return FV2D_ERR_INVALID;
   if (cfg->max_sims <= 0 || cfg->max_sims > 16384 || !(cfg->budget_bytes > 0)) return FV2D_ERR_INVALID;

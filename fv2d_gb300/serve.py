@@ -60,6 +60,8 @@ def _bind(L):
     L.fv2d_server_set_tile_wait_limit.argtypes = [vp, C.c_uint32]
     L.fv2d_server_config_name.argtypes = [C.c_int]
     L.fv2d_server_config_name.restype = C.c_char_p
+    L.fv2d_server_config_families.argtypes = [C.c_int]
+    L.fv2d_server_config_families.restype = C.c_int
     L._serve_bound = True
     return L
 
@@ -75,6 +77,18 @@ def check_request(req):
 def config_name(index):
     v = _bind(_lib_loader()).fv2d_server_config_name(index)
     return v.decode() if v else None
+
+
+FAMILIES = ("plain", "diffusive", "extended")
+
+
+def config_families(name):
+    """The kernel families (of FAMILIES) that configuration `name` serves."""
+    names = config_names()
+    if name not in names:
+        raise ValueError(f"unknown configuration {name!r}; known: {names}")
+    mask = _bind(_lib_loader()).fv2d_server_config_families(names.index(name))
+    return [f for k, f in enumerate(FAMILIES) if (mask >> k) & 1]
 
 
 def config_names():

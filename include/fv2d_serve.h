@@ -161,8 +161,15 @@ int fv2d_server_inject_fault(fv2d_server *s);
  * does.  Applied by the worker before its next replay. */
 int fv2d_server_set_tile_wait_limit(fv2d_server *s, uint32_t polls);
 
-/* Name of tile configuration `index` ("32x16/256/tma", ...); NULL if none. */
+/* Name of kernel configuration `index` ("32x16/256/tma", "28/32x20/march", "60/32x16/march2", ...); NULL if
+ * none.  The names of the march kernels read <strip columns>/<threads per CTA>x<CTAs per SM>/<kernel>. */
 const char *fv2d_server_config_name(int index);
+
+/* Kernel families configuration `index` serves, as a bit mask: 1 plain (HLL / HLLC, PCM / PLM, constant
+ * gravity), 2 diffusive (the same with constant conduction and / or viscosity), 4 extended (FSLP,
+ * MUSCL-Hancock, analytical gravity, B02 conductivity, the y-boundary conduction modes, the well-balanced y
+ * flux); -1 if there is no such configuration.  Needs no GPU. */
+int fv2d_server_config_families(int index);
 
 #ifdef __cplusplus
 }

@@ -188,3 +188,23 @@ def test_server_request_checks_without_a_server(libs):
     assert lib.fv2d_server_check_request(None, buf, 64) == _abi.ERR_INVALID
     assert lib.fv2d_server_check_request(C.byref(req()), None, 0) == _abi.OK
     assert lib.fv2d_server_check_request(C.byref(req()), buf, -1) == _abi.ERR_INVALID
+
+
+def test_kernel_configurations_without_gpu(libs):
+    """The service's kernel configurations: unique names, every kernel
+    family served by at least one, the march kernels named by strip,
+    threads per CTA and CTAs per SM, and a plain-only two-column one."""
+    from fv2d_gb300.serve import config_names, config_families, FAMILIES, _bind
+    names = config_names()
+    assert len(names) == len(set(names)) and len(names) >= 3
+    fams = {n: config_families(n) for n in names}
+    for f in FAMILIES:
+        assert any(f in v for v in fams.values()), f
+    assert all(fams[n] for n in names)
+    assert fams["60/32x16/march2"] == ["plain"]
+    assert fams["60/32x10/march2-diff"] == ["diffusive"]
+    assert fams["28/32x20/march"] == ["plain", "diffusive"]
+    assert fams["28/64x8/march-ext"] == ["extended"]
+    lib = _bind(libs)
+    assert lib.fv2d_server_config_families(-1) == -1
+    assert lib.fv2d_server_config_families(len(names)) == -1
