@@ -219,6 +219,8 @@ def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, de
     wall = time.perf_counter() - t_start
     st = srv.stats()
     cfgs = [config_name(st.bucket_cfg[b]) for b in range(4)]
+    fam_cfgs = {"plain": config_name(st.bucket_cfg[0]), "diffusive": config_name(st.diff_cfg[0]),
+                "extended": config_name(st.ext_cfg)}
     srv.close()
     tts = np.array([results[i].done_s - results[i].submit_s for i in range(len(reqs))])
     work = sum(float(r["N"]) ** 2 * results[i].steps for i, r in enumerate(reqs))
@@ -257,7 +259,8 @@ def run_served(fv, n_requests=512, rate=200.0, sample_every=16, budget=150e9, de
         "requests": len(reqs), "arrival_rate_hz": rate, "aggregate": agg, "unit": METRIC, "dtype": "f32 state/flux, "
         "f64 clock/dt/conservation sums/low-Mach energy recovery", "wall_s": wall, "cell_updates": work,
         "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
-        "tile_configs_per_bucket": cfgs, "replays": st.replays, "arena_reserved_gb": st.bytes_reserved / 1e9,
+        "tile_configs_per_bucket": cfgs, "kernel_configurations": fam_cfgs, "replays": st.replays,
+        "arena_reserved_gb": st.bytes_reserved / 1e9,
         "scheduling": ("shortest remaining work first, about %.3g cells per step" % active_cells) if active_cells > 0
         else "every admitted request at every step",
         "plain_fp64_one_at_a_time": {"sample": len(sub), "aggregate": plain_rate, "unit": METRIC,
