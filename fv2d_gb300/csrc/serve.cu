@@ -58,11 +58,6 @@ constexpr int kLanes = kFamilies * kBuckets;
 int num_cfgs() { return batch_num_cfgs(); }
 constexpr int kConsBlocks = 64;
 constexpr int kMinSide = 16, kMaxSide = 8192;  // accepted Nx, Ny
-// Band heights the march lanes choose from (rows per work item), tallest
-// first, and the work items per resident warp a lane's launch should have.
-constexpr int kBands[] = {32, 24, 16, 12, 8};
-constexpr int kMinBand = 8;
-constexpr double kItemsPerWarp = 2.0;
 static_assert(offsetof(SimDev, band) == offsetof(SimDev, nty) + sizeof(int), "nty and band are updated by one copy");
 
 // Grid-size bucket of an Nx x Ny grid, by its cell count (the side of the
@@ -641,31 +636,20 @@ double remaining_work(const fv2d_server *s, int slot) {
   return std::max(steps, 1.0) * cells;
 }
 
-// Band height of a march lane for the simulations it is about to run: the
-// tallest of kBands that gives the launch at least kItemsPerWarp work items
-// per resident warp, else the shortest.  Measured on single grids (one
-// simulation in the lane; KH 4096^2 and RT 1024 x 3072, bands 12..64) and on
-// batches of 12 and 40 Sedov 768^2 grids: the rate falls by 10-20 % when the
-// items end within one or a little over one wave of the resident warps (the
-// last warps run alone, or every warp runs its one item in step with the
-// others), by a few per cent still at 1.5 items per warp, while the extra
-// window fill of a shorter band costs a few per cent; bands taller than 32
-// rows gained nothing where the items were plentiful and lost 9 % at 64.  A
-// simulation's results do not depend on the band: every face is computed by
-// the same code whichever band holds it.
-int choose_band(const fv2d_server *s, int lane, const std::vector<int> &slots) {
+// Band height of a march lane for the simulations it is about to run
+// (schedule.hpp); the tile kernels keep their tile height.  A simulation's
+// results do not depend on the band: every face is computed by the same code
+// whichever band holds it.
+int lane_band(const fv2d_server *s, int lane, const std::vector<int> &slots) {
   const int c = lane_cfg(s, lane);
   int tx, ty, nt, staging;
   batch_cfg_info(c, &tx, &ty, &nt, &staging, nullptr, nullptr, nullptr);
-  if (staging != 2 || slots.empty()) return ty;  // tile kernels: the tile height
+  if (staging != 2 || slots.empty()) return ty;
   if (s->cfg.band_rows > 0) return s->cfg.band_rows;
-  const double warps = (double)s->cfg_grid[c] * (nt / 32);
-  for (int H : kBands) {
-    double items = 0;
-    for (int k : slots) items += (double)s->h_up[k].ntx * ((s->h_up[k].Ny + H - 1) / H);
-    if (items >= kItemsPerWarp * warps) return H;
-  }
-  return kMinBand;
+  std::vector<BandGrid> grids;
+  grids.reserve(slots.size());
+  for (int k : slots) grids.push_back(BandGrid{s->h_up[k].ntx, s->h_up[k].Ny});
+  return choose_band(grids, (double)s->cfg_grid[c] * (nt / 32));
 }
 
 void rebuild_lists(fv2d_server *s) {
@@ -690,7 +674,7 @@ void rebuild_lists(fv2d_server *s) {
   }
   s->mask = 0;
   for (int b = 0; b < kLanes; ++b) {
-    const int band = choose_band(s, b, per_lane[b]);
+    const int band = lane_band(s, b, per_lane[b]);
     for (int slot : per_lane[b]) {
       SimDev &u = s->h_up[slot];
       if (u.band != band) {  // nty and band, adjacent in the table entry

@@ -59,3 +59,35 @@ def test_shortest_remaining_work_first_matches_the_policy(harness):
         if cands and cap > 0:
             chosen = sum(c for s, _, c in cands if s in got)
             assert got and (chosen >= cap or len(got) == len(cands))
+
+
+def band_rule(grids, warps):
+    """The march lanes' band height: the tallest of 32, 24, 16, 12, 8 rows
+    that gives the launch at least 2 work items per resident warp, else 8."""
+    for H in (32, 24, 16, 12, 8):
+        if sum(s * -(-ny // H) for s, ny in grids) >= 2.0 * warps:
+            return H
+    return 8
+
+
+def test_band_height_matches_the_rule(harness):
+    rng = np.random.default_rng(11)
+    # single grids the benchmark runs: RT 1024 x 3072 on the one-column march
+    # (37 strips of 28, 3040 resident warps) takes 16 rows; KH 4096^2 on the
+    # two-column one (69 strips of 60, 2432 warps) 32 rows; a lone 64^2 grid 8
+    cases = [([(37, 3072)], 3040.0), ([(69, 4096)], 2432.0), ([(3, 64)], 3040.0), ([(13, 768)] * 12, 2432.0)]
+    expect = [16, 32, 8, 24]
+    for _ in range(300):
+        n = int(rng.integers(1, 60))
+        strip = int(rng.choice([28, 60]))
+        Ns = rng.integers(16, 2049, size=n)
+        grids = [(-(-int(rng.integers(16, 2049)) // strip), int(N)) for N in Ns]
+        cases.append((grids, float(rng.choice([2432.0, 3040.0, 1216.0]))))
+    text = "".join(f"{len(g)} {w!r}\n" + "".join(f"{s} {ny}\n" for s, ny in g) for g, w in cases)
+    r = subprocess.run([harness, "band"], input=text, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    got = [int(x) for x in r.stdout.split()]
+    assert len(got) == len(cases)
+    assert got[:len(expect)] == expect
+    for (grids, warps), h in zip(cases, got):
+        assert h == band_rule(grids, warps), (grids, warps)
