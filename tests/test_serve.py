@@ -376,3 +376,26 @@ def test_many_small_requests(gpu_lib, active):
             s.release(rid)
         st = s.stats()
         assert st.active == 0 and st.completed == len(reqs) and st.bytes_in_use == 0
+
+
+def test_autotuner_keeps_one_configuration_per_family(gpu_lib):
+    """The autotuner times the candidates of the plain and the diffusive
+    families and keeps, per family, one configuration for every bucket, one
+    that serves the family; requests then run in their family's lanes."""
+    import fv2d_gb300 as fv
+    from fv2d_gb300.serve import Server, config_name, config_families
+    with Server(budget_bytes=2e9, autotune=True) as s:
+        st = s.stats()
+        plain = {config_name(c) for c in st.bucket_cfg}
+        diff = {config_name(c) for c in st.diff_cfg}
+        assert len(plain) == 1 and "plain" in config_families(plain.pop())
+        assert len(diff) == 1 and "diffusive" in config_families(diff.pop())
+        assert "extended" in config_families(config_name(st.ext_cfg))
+        reqs = [("sedov", params(96), 20), ("rt_hydrostatic", rt_rect(), 20),
+                ("sod_x", params(64, Ny=32, boundary_x=fv.BC_ABSORBING, boundary_y=fv.BC_PERIODIC,
+                                 riemann_solver=fv.FSLP), 20)]
+        ids = [s.submit(pb, p, n) for pb, p, n in reqs]
+        assert s.drain(120) == 0
+        res = {r.id: r for r in s.poll()}
+        assert [res[i].lane // 4 for i in ids] == [0, 1, 2]
+        assert all(res[i].status == 0 and res[i].steps == 20 for i in ids)
